@@ -1,0 +1,368 @@
+"""Benchmark: batched FD1D American-option pricing on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one "step"): one batch of 32768 American options (half puts, half calls,
+S=100, K~U[80,120], vol~U[0.1,0.6], r,q~U[0,0.1], T~U[0.25,2]), 1024 x 1024 grid,
+theta 0.5, scale 5, uniform x-grid, FP64 -- the reference's largest logged shape
+(log/z800_1024_32768.log).  Synthetic, seeded (kwinto-cuda_gb300/portfolio.py).
+
+Reported on one JSON line (rank 0):
+  value      options/s with inputs resident in HBM (kwg_fd1d_price_device), CUDA
+             events on the launching stream, K steps after W warm-up steps; the
+             per-step working set (2.7 GB of coefficients and state) is far larger
+             than L2, so no flush is needed between steps.
+  e2e        the same metric through the reference-facing call (kwg_fd1d_price: host
+             options in, host prices out; dedup, H2D and D2H inside the timing).
+  roofline   of the solve kernel, from its own CUDA events inside the timed region.
+  variants   FP64 and FP32 rates and their errors against the FP64 oracle.
+  cpu_baseline  the oracle (C restatement of the reference, all host cores) on a
+             bounded sample of the same workload.
+With --impl reference the reference's CPU implementation runs instead (oracle/_ref
+when it was built here from the reference sources, else the oracle port).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "kwinto-cuda_gb300"))
+
+N_OPTIONS = 32768
+X_DIM = T_DIM = 1024
+SCALE = 5.0
+DENSITY = math.inf  # uniform grid
+WORKLOAD = "fd1d_american_32768x1024x1024"
+# The reference's own FD64 number for this exact shape (log/z800_1024_32768.log:87-93,
+# GTX 1070): 32768 options per 39,901.747 ms.
+REF_PUBLISHED_OPS = 32768 / 39.901747
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def node_steps(n, x_dim=X_DIM, t_dim=T_DIM):
+    return n * x_dim * (t_dim - 1)
+
+
+# Algorithmic traffic of the FP64 streaming solve per node and step: V and the sweep
+# value read and written (4 x 8 B), four factor coefficients read (4 x 8 B).
+FP64_BYTES_PER_NODE_STEP = 64
+FP64_FLOPS_PER_NODE_STEP = 8  # 3 FMA + 1 MUL
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = os.path.join("/tmp", f"kwg_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        d = json.load(open(PEAKS_FILE))
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def cpu_oracle_rate(opts_all, budget_s=12.0):
+    """The oracle (C restatement, all host cores) on a bounded sample of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import kwor
+
+    threads = os.cpu_count() or 1
+    n = 32
+    while True:
+        sample = opts_all[:n]
+        t0 = time.perf_counter()
+        rc, msg, _, _ = kwor.fd1d_price(sample, nthreads=threads, t_dim=T_DIM, x_dim=X_DIM, scale=SCALE,
+                                        density=DENSITY)
+        dt = time.perf_counter() - t0
+        if rc != 0:
+            raise RuntimeError(msg)
+        if dt >= budget_s / 4 or n >= len(opts_all):
+            return n / dt, threads, n, dt
+        n = min(len(opts_all), int(n * max(2.0, budget_s / 4 / max(dt, 1e-3))))
+
+
+def fp64_error_sample(opts, gpu_prices, k=64):
+    """Max relative error of GPU FP64 prices against the oracle on an evenly spaced sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import kwor
+
+    idx = np.linspace(0, len(opts) - 1, k).astype(int)
+    rc, msg, want, _ = kwor.fd1d_price(opts[idx], t_dim=T_DIM, x_dim=X_DIM, scale=SCALE, density=DENSITY)
+    if rc != 0:
+        raise RuntimeError(msg)
+    return float(np.max(np.abs(gpu_prices[idx] - want) / np.abs(want))), int(k)
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU implementation on the host cores."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import kwor
+    import portfolio
+
+    threads = os.cpu_count() or 1
+    per_step = args.ref_options
+    use_ref = kwor.ref_available()
+    kind = "reference" if use_ref else "port"
+
+    def one(i):
+        o = portfolio.config1_like(per_step, seed=42, start=(i * per_step) % N_OPTIONS)
+        t0 = time.perf_counter()
+        if use_ref:
+            rc, msg, _, _ = kwor.ref_price(o, density=portfolio.REFERENCE_UNIFORM_DENSITY, scale=SCALE,
+                                           t_dim=T_DIM, x_dim=X_DIM)
+        else:
+            rc, msg, _, _ = kwor.fd1d_price(o, nthreads=threads, t_dim=T_DIM, x_dim=X_DIM, scale=SCALE,
+                                            density=DENSITY)
+        if rc != 0:
+            raise RuntimeError(msg)
+        return time.perf_counter() - t0
+
+    for i in range(args.warmup):
+        one(i)
+    total = sum(one(args.warmup + i) for i in range(args.steps))
+    value = per_step * args.steps / total
+    cores = kwor.ref_lib().kwref_pool_size() if use_ref else threads
+    sample = (f"{per_step} options per step of the {N_OPTIONS}-option batch, 1024x1024, "
+              + ("reference src/ compiled from source, density 1e6 (its closest to uniform)" if use_ref
+                 else "oracle C restatement, uniform grid"))
+    line = {
+        "impl": "reference", "metric": "options_per_sec_fd64_1024x1024", "value": value, "unit": "options/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": value / REF_PUBLISHED_OPS, "dtype": "f64",
+        "data": "synthetic (seeded splitmix64, config-2 distributions)",
+        "config": {"workload": WORKLOAD, "options_per_batch": N_OPTIONS, "x_dim": X_DIM, "t_dim": T_DIM,
+                   "theta": 0.5, "scale": SCALE, "grid": "uniform", "precision": "fp64"},
+        "cpu_baseline": {"value": value, "unit": "options/s", "cores": cores, "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": "options/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    import kwg
+    import portfolio
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ctx = kwg.Context(local)
+    stream = torch.cuda.current_stream(dev)
+
+    # each rank prices its own batch (weak scaling), drawn from its own window of the stream
+    opts = portfolio.config1_like(N_OPTIONS, seed=42, start=rank * N_OPTIONS)
+    prm = kwg.params(t_dim=T_DIM, x_dim=X_DIM, scale=SCALE, density=DENSITY, precision=kwg.FP64)
+    d_opts = torch.from_numpy(opts.view(np.uint8).copy()).to(dev)
+    d_prices = torch.empty(N_OPTIONS, dtype=torch.float64, device=dev)
+    d_status = torch.empty(N_OPTIONS, dtype=torch.int32, device=dev)
+
+    def step():
+        rc = ctx.fd1d_price_device(d_opts.data_ptr(), N_OPTIONS, prm, d_prices.data_ptr(), d_status.data_ptr(),
+                                   stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError(ctx.last_error())
+        return ctx.launch_count()
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    def max_over_ranks(x):
+        if ws == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---------------------------------------------------------------- resident (value)
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    ctx.set_profiling(True)
+    clocks = Clocks(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        launches += step()
+    e1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    solve_ms, solve_n = ctx.profile_read()
+    ctx.set_profiling(False)
+    ms = max_over_ranks(e0.elapsed_time(e1))
+    value = ws * N_OPTIONS * args.steps / (ms / 1e3)
+    status = d_status.cpu().numpy()
+    gpu_prices = d_prices.cpu().numpy()
+    if not (status == 0).all():
+        raise RuntimeError(f"{int((status != 0).sum())} options failed")
+
+    # ---------------------------------------------------------------- end to end (e2e)
+    prices_host = np.empty(N_OPTIONS)
+    for _ in range(max(1, args.warmup)):
+        rc, prices_host, _ = ctx.fd1d_price(opts, prm)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        rc, prices_host, st = ctx.fd1d_price(opts, prm)
+        if rc != 0:
+            raise RuntimeError(ctx.last_error())
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    barrier()
+    e2e_value = ws * N_OPTIONS * args.steps / e2e_s
+    if not np.array_equal(prices_host, gpu_prices):
+        raise RuntimeError("host and device entry points disagree")
+    # bytes the host call moves per step (include/kwg.h packing): per PDE t,z,r,q (f64) + w,e;
+    # per asset s,k (f64) + pde index (i32); back: price (f64) + status (i32) per asset.
+    h2d = N_OPTIONS * (4 * 8 + 2) + N_OPTIONS * (2 * 8 + 4)
+    d2h = N_OPTIONS * (8 + 4)
+
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    if rank != 0:
+        return
+
+    # ---------------------------------------------------------------- roofline (solve kernel)
+    hbm, peak_src = peaks()
+    per_launch_s = solve_ms / 1e3 / max(solve_n, 1)
+    ns = node_steps(N_OPTIONS)
+    achieved = FP64_BYTES_PER_NODE_STEP * ns / per_launch_s / 1e9
+    fp64_tflops = FP64_FLOPS_PER_NODE_STEP * ns / per_launch_s / 1e12
+    traffic = None
+    prof_file = os.path.join(ROOT, "profiles", "fd1d_solve_fp64_traffic.json")
+    if os.path.exists(prof_file):
+        try:
+            traffic = json.load(open(prof_file)).get("bytes_per_launch_full_size")
+        except ValueError:
+            traffic = None
+
+    err, nerr = fp64_error_sample(opts, gpu_prices)
+    if err > 1e-10:
+        raise RuntimeError(f"FP64 parity broken: max rel err {err:.3e} > 1e-10")
+    cpu_rate, cpu_threads, cpu_n, cpu_s = cpu_oracle_rate(opts) if not args.no_cpu else (None, 0, 0, 0.0)
+
+    line = {
+        "metric": "options_per_sec_fd64_1024x1024",
+        "value": value,
+        "unit": "options/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": value / REF_PUBLISHED_OPS,
+        "dtype": "f64",
+        "data": "synthetic (seeded splitmix64, config-2 distributions)",
+        "config": {"workload": WORKLOAD, "options_per_batch": N_OPTIONS, "x_dim": X_DIM, "t_dim": T_DIM,
+                   "theta": 0.5, "scale": SCALE, "grid": "uniform", "precision": "fp64", "solver": "thomas",
+                   "l2": "working set 2.7 GB per step > 129 MB L2 (no flush needed)"},
+        "e2e": {"value": e2e_value, "unit": "options/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "roofline": {"bound": "hbm", "kernel": "fd1d_solve_fp64", "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_src, "traffic": traffic,
+                     "algorithmic_bytes_per_node_step": FP64_BYTES_PER_NODE_STEP,
+                     "node_steps_per_launch": ns, "launch_ms": per_launch_s * 1e3,
+                     "fp64_tflops": fp64_tflops},
+        "cpu_baseline": ({"value": cpu_rate, "unit": "options/s", "cores": cpu_threads, "kind": "port",
+                          "sample": f"{cpu_n} options of the batch at 1024x1024 ({cpu_s:.1f} s), oracle C "
+                                    f"restatement, {cpu_threads} threads"} if cpu_rate else None),
+        "variants": {"fd64": {"options_per_sec": value, "max_rel_err_vs_oracle": err,
+                              "oracle_sample": nerr}},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--ref-options", type=int, default=256, help="options per reference step")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--options", type=int, default=N_OPTIONS,
+                    help="options per batch (default 32768; smaller values are for profiling captures)")
+    args = ap.parse_args()
+    globals()["N_OPTIONS"] = args.options
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

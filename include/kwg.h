@@ -1,0 +1,125 @@
+/*
+ * kwg.h -- C ABI of the GB300 batched finite-difference American-option pricer.
+ *
+ * This is the drop-in boundary for the FD1D solve of gituliar/kwinto-cuda.  The
+ * reference exposes it as the C++ interface
+ *     kw::Pricer::init(const Config&)                                src/Pricer/kwPricer.h:14-16
+ *     kw::Pricer::price(const vector<Option>&, vector<double>&)      src/Pricer/kwPricer.h:18-20
+ *     kw::PricerFactory::create(config, pricer)  (PRICER=FD1D)       src/Pricer/kwPricerFactory.h:15-41
+ * over the solver
+ *     kw::Fd1d::solve / kw::Fd1d::value                              src/Math/kwFd1d.h:49-52
+ * Every entry point below takes plain pointers and sizes; errors are returned as an
+ * int status (0 = success) with the message in kwg_last_error(), the C form of the
+ * reference's kw::Error string (src/Core/kwTypes.h:15, empty = OK).
+ *
+ * Threading: a kwg_ctx owns device buffers and one CUDA stream; like a reference
+ * pricer object (src/Pricer/kwFd1d.h:22-30) it is stateful and not re-entrant --
+ * use one context per calling thread.
+ */
+#ifndef KWG_H
+#define KWG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes ---------------------------------------------------------------- */
+#define KWG_OK 0
+#define KWG_ERR_INVALID 1     /* bad argument (null pointer, grid too small, theta out of range) */
+#define KWG_ERR_CUDA 2        /* a CUDA call failed; message has the CUDA error string */
+#define KWG_ERR_OUT_OF_GRID 3 /* strict mode: an asset's log(s/k) lies outside its x-grid */
+#define KWG_ERR_SOLVER 4      /* strict mode: a tridiagonal pivot was zero or not finite */
+
+/* ---- per-option status (status[i]) --------------------------------------------------- */
+#define KWG_STATUS_OK 0
+#define KWG_STATUS_OUT_OF_GRID 1 /* price is NaN; the reference fails the whole batch here */
+#define KWG_STATUS_SOLVER 2      /* price is NaN; zero/non-finite pivot in the factorisation */
+#define KWG_STATUS_BAD_INPUT 3   /* price is NaN; t<=0, z<=0, k<=0 or s<=0 */
+
+/* ---- numeric modes ------------------------------------------------------------------- */
+#define KWG_FP64 0 /* all stepping in FP64: parity with the reference to <= 1e-10 relative */
+#define KWG_FP32 1 /* FP32 stepping with FP64-accurate state and residual (see DESIGN) */
+
+#define KWG_SOLVER_AUTO 0
+#define KWG_SOLVER_THOMAS 1 /* thread per option, option-interleaved streaming layout */
+#define KWG_SOLVER_PCR 2    /* warp per option, partitioned solve with shuffles, state on chip */
+
+/* Same field order, types and 56-byte layout as kw::Option (src/Core/kwAsset.h:12-22). */
+typedef struct kwg_option {
+    double t; /* time to maturity, years          */
+    double k; /* strike                           */
+    double z; /* volatility                       */
+    double r; /* interest rate                    */
+    double q; /* dividend rate                    */
+    double s; /* spot                             */
+    uint8_t e; /* early exercise: 0 European, 1 American */
+    int8_t w;  /* -1 put, +1 call                 */
+} kwg_option;
+
+/* The FD1D.* config keys of the reference (src/Pricer/kwFd1d.cpp:12-16) plus the
+ * GPU knobs.  Defaults (kwg_fd1d_params_default) are the reference defaults. */
+typedef struct kwg_fd1d_params {
+    int32_t t_dim;     /* FD1D.T_GRID_SIZE, default 512 (>= 2) */
+    int32_t x_dim;     /* FD1D.X_GRID_SIZE, default 512 (>= 3) */
+    double theta;      /* theta of the scheme, default 0.5 (the reference hard-codes it,
+                          src/Math/kwFd1d.h:31); any value in (0, 1]        */
+    double scale;      /* FD1D.SCALE, default 50: half-width scale*z*sqrt(t) */
+    double density;    /* FD1D.DENSITY, default 0.25; +INFINITY = uniform grid (the
+                          density -> infinity limit of the sinh grid)        */
+    int32_t precision; /* KWG_FP64 (default) or KWG_FP32 */
+    int32_t solver;    /* KWG_SOLVER_AUTO (default), _THOMAS or _PCR */
+    int32_t strict;    /* 1: return an error for the first bad option, like the
+                          reference (src/Pricer/kwFd1d.cpp:154-155); 0 (default):
+                          per-option status and NaN, the batch still succeeds */
+    int32_t reserved;
+} kwg_fd1d_params;
+
+typedef struct kwg_ctx kwg_ctx;
+
+/* Fills p with the reference defaults (src/Pricer/kwFd1d.cpp:12-16, kwFd1d.h:31). */
+void kwg_fd1d_params_default(kwg_fd1d_params* p);
+
+/* Creates a context on CUDA device `device`; NULL on failure (no GPU, bad id). */
+kwg_ctx* kwg_create(int device);
+void kwg_destroy(kwg_ctx* ctx);
+
+/* Message of the last failed call on ctx ("" if it succeeded). */
+const char* kwg_last_error(const kwg_ctx* ctx);
+
+/* Prices n options given in HOST memory; writes n prices (and, if status is not
+ * NULL, n per-option status codes) to HOST memory.  Blocking.
+ * Replaces kw::Fd1d_Pricer::price (src/Pricer/kwFd1d.cpp:21-160): the options are
+ * deduplicated by (t,r,q,z,e,w) on the host exactly like the reference
+ * (src/Pricer/kwFd1d.cpp:28-65), one PDE is solved per distinct key on the GPU, and
+ * prices[i] = k * V(log(s/k)) by linear interpolation (src/Math/kwFd1d.cpp:139-158).
+ * n == 0 succeeds and writes nothing. */
+int kwg_fd1d_price(kwg_ctx* ctx, const kwg_option* opts, size_t n, const kwg_fd1d_params* p,
+                   double* prices, int32_t* status);
+
+/* Same computation with inputs and outputs already in DEVICE memory and no
+ * deduplication (every option is solved as its own PDE).  Asynchronous on `stream`
+ * (a cudaStream_t; NULL = the context's stream).  For callers that keep portfolios
+ * resident in HBM.  Replaces kw::Fd1d::solve + kw::Fd1d::value
+ * (src/Math/kwFd1d.cpp:11-58, 139-158). */
+int kwg_fd1d_price_device(kwg_ctx* ctx, const kwg_option* d_opts, size_t n,
+                          const kwg_fd1d_params* p, double* d_prices, int32_t* d_status,
+                          void* stream);
+
+/* Number of kernel launches the last pricing call made (for launch accounting). */
+int kwg_last_launch_count(const kwg_ctx* ctx);
+
+/* Kernel timing for roofline accounting.  With profiling on, every pricing call
+ * records CUDA events around its solve kernel on the stream it launches on;
+ * kwg_profile_read waits for them, returns the summed solve-kernel time (ms) and the
+ * number of launches since the last read, and starts a new accumulation. */
+int kwg_set_profiling(kwg_ctx* ctx, int enable);
+int kwg_profile_read(kwg_ctx* ctx, double* solve_ms, int* solve_launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KWG_H */

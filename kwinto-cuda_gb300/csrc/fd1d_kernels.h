@@ -1,0 +1,61 @@
+// fd1d_kernels.h -- host-visible launch interface of the FD1D kernels (internal to
+// libkwg.so; the public boundary is include/kwg.h).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace kwg {
+
+constexpr int kTile = 32;  // PDEs per tile: one warp, one PDE per lane
+
+// One PDE per distinct option key (t, r, q, z, e, w), structure-of-arrays in device
+// memory; m PDEs, padded to m_pad = a multiple of 32 (padding lanes replicate PDE m-1).
+struct PdeBatch {
+    const double* t;
+    const double* z;
+    const double* r;
+    const double* q;
+    const int8_t* w;
+    const uint8_t* e;
+    int m;
+    int m_pad;
+};
+
+// Assets to price: spot, strike and the PDE slot each one reads its value from.
+struct AssetBatch {
+    const double* s;
+    const double* k;
+    const int32_t* pde;
+    int n;
+};
+
+// Grid shape and scheme parameters shared by a batch.
+struct Fd1dShape {
+    int x_dim;
+    int t_dim;
+    double theta;
+    double c;  // (1 - theta) / theta
+    double scale;
+    double density;
+    bool uniform;
+};
+
+size_t fd1d_fp64_coef_bytes(int m_pad, int x_dim);
+size_t fd1d_fp64_state_bytes(int m_pad, int x_dim);
+
+// Optional CUDA events recorded immediately before and after the solve kernel.
+struct SolveEvents {
+    cudaEvent_t start = nullptr, stop = nullptr;
+};
+
+// Launches setup, solve and interpolation on `stream`; returns the launch count.
+int fd1d_fp64_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* coef, double* state,
+                     int32_t* pde_status, int* tile_counter, double* prices, int32_t* status, int solve_blocks,
+                     cudaStream_t stream, const SolveEvents* ev);
+
+// Occupancy-derived persistent grid size for the FP64 solve kernel.
+int fd1d_fp64_solve_blocks(int ntiles, int device);
+
+}  // namespace kwg

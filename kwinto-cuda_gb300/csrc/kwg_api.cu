@@ -1,0 +1,415 @@
+// kwg_api.cu -- the C ABI of include/kwg.h: context, host-side deduplication,
+// staging, launches and error mapping.
+//
+// Host flow of kwg_fd1d_price, mirroring kw::Fd1d_Pricer::price
+// (src/Pricer/kwFd1d.cpp:21-160):
+//   1. dedup the options by (t, r, q, z, e, w) like src/Pricer/kwFd1d.cpp:28-65;
+//   2. pack PDE and asset arrays into one pinned buffer, one H2D copy;
+//   3. setup + solve + interpolation kernels on the context stream;
+//   4. one D2H copy of (prices, status); strict mode maps the first bad option to
+//      the reference's whole-call error (src/Pricer/kwFd1d.cpp:154-155).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "fd1d_kernels.h"
+#include "kwg.h"
+
+struct kwg_ctx {
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int launches = 0;
+
+    // grow-only device buffers
+    void* d_work = nullptr;  // coefficients + state
+    size_t work_bytes = 0;
+    void* d_io = nullptr;  // packed inputs / outputs
+    size_t io_bytes = 0;
+    int* d_counter = nullptr;
+    // pinned host staging
+    void* h_io = nullptr;
+    size_t h_io_bytes = 0;
+    // solve-kernel timing (kwg_set_profiling)
+    bool profiling = false;
+    std::vector<kwg::SolveEvents> events;  // pool, reused across reads
+    size_t events_used = 0;
+
+    const kwg::SolveEvents* next_events()
+    {
+        if (!profiling) return nullptr;
+        if (events_used == events.size()) {
+            kwg::SolveEvents e;
+            if (cudaEventCreate(&e.start) != cudaSuccess || cudaEventCreate(&e.stop) != cudaSuccess) return nullptr;
+            events.push_back(e);
+        }
+        return &events[events_used++];
+    }
+};
+
+namespace {
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+int set_err(kwg_ctx* ctx, int code, const std::string& msg)
+{
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+int cuda_err(kwg_ctx* ctx, cudaError_t e, const char* what)
+{
+    return set_err(ctx, KWG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define KWG_CUDA(ctx, call)                                   \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_err(ctx, e_, #call); \
+    } while (0)
+
+int ensure_device(kwg_ctx* ctx, void** buf, size_t* cap, size_t need)
+{
+    if (need <= *cap) return KWG_OK;
+    if (*buf) cudaFree(*buf);
+    *buf = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc(buf, need);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "cudaMalloc");
+    *cap = need;
+    return KWG_OK;
+}
+
+int ensure_host(kwg_ctx* ctx, void** buf, size_t* cap, size_t need)
+{
+    if (need <= *cap) return KWG_OK;
+    if (*buf) cudaFreeHost(*buf);
+    *buf = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMallocHost(buf, need);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "cudaMallocHost");
+    *cap = need;
+    return KWG_OK;
+}
+
+int check_params(kwg_ctx* ctx, const kwg_fd1d_params* p)
+{
+    if (!p) return set_err(ctx, KWG_ERR_INVALID, "kwg: null params");
+    if (p->x_dim < 3) return set_err(ctx, KWG_ERR_INVALID, "kwg: x_dim must be >= 3");
+    if (p->t_dim < 2) return set_err(ctx, KWG_ERR_INVALID, "kwg: t_dim must be >= 2");
+    if (!(p->theta > 0.) || !(p->theta <= 1.))
+        return set_err(ctx, KWG_ERR_INVALID, "kwg: theta must be in (0, 1]");
+    if (!(p->scale > 0.) || !std::isfinite(p->scale))
+        return set_err(ctx, KWG_ERR_INVALID, "kwg: scale must be positive and finite");
+    if (!(p->density > 0.)) return set_err(ctx, KWG_ERR_INVALID, "kwg: density must be positive");
+    if (p->precision != KWG_FP64 && p->precision != KWG_FP32)
+        return set_err(ctx, KWG_ERR_INVALID, "kwg: unknown precision");
+    if (p->solver < KWG_SOLVER_AUTO || p->solver > KWG_SOLVER_PCR)
+        return set_err(ctx, KWG_ERR_INVALID, "kwg: unknown solver");
+    if (p->precision == KWG_FP32)
+        return set_err(ctx, KWG_ERR_INVALID, "kwg: FP32 stepping is not available in this build");
+    if (p->solver == KWG_SOLVER_PCR)
+        return set_err(ctx, KWG_ERR_INVALID, "kwg: the PCR solver is not available in this build");
+    return KWG_OK;
+}
+
+kwg::Fd1dShape make_shape(const kwg_fd1d_params* p)
+{
+    kwg::Fd1dShape sh;
+    sh.x_dim = p->x_dim;
+    sh.t_dim = p->t_dim;
+    sh.theta = p->theta;
+    sh.c = (1. - p->theta) / p->theta;
+    sh.scale = p->scale;
+    sh.uniform = std::isinf(p->density);
+    sh.density = sh.uniform ? 1. : p->density;
+    return sh;
+}
+
+// Device pointers into one packed buffer holding a batch's inputs and outputs.
+struct IoLayout {
+    size_t t, z, r, q, s, k, pde, w, e, prices, status, pde_status, total;
+    size_t in_bytes;   // [0, in_bytes) is copied host -> device
+    size_t out_bytes;  // [prices, prices + out_bytes) is copied device -> host
+};
+
+IoLayout io_layout(size_t m, size_t m_pad, size_t n)
+{
+    IoLayout L;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = o;
+        o = align_up(o + bytes, 256);
+        return at;
+    };
+    L.t = take(m * 8);
+    L.z = take(m * 8);
+    L.r = take(m * 8);
+    L.q = take(m * 8);
+    L.s = take(n * 8);
+    L.k = take(n * 8);
+    L.pde = take(n * 4);
+    L.w = take(m);
+    L.e = take(m);
+    L.in_bytes = o;
+    L.prices = take(n * 8);
+    L.status = take(n * 4);
+    L.out_bytes = o - L.prices;
+    L.pde_status = take(m_pad * 4);
+    L.total = o;
+    return L;
+}
+
+// AoS kw::Option layout in device memory -> the SoA arrays of one packed buffer.
+__global__ void unpack_options(const kwg_option* __restrict__ o, int n, double* t, double* z, double* r,
+                               double* q, double* s, double* k, int32_t* pde, int8_t* w, uint8_t* e)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const kwg_option a = o[i];
+    t[i] = a.t;
+    z[i] = a.z;
+    r[i] = a.r;
+    q[i] = a.q;
+    s[i] = a.s;
+    k[i] = a.k;
+    pde[i] = i;
+    w[i] = a.w;
+    e[i] = a.e;
+}
+
+int run_batch(kwg_ctx* ctx, char* io, const IoLayout& L, int m, int n, const kwg_fd1d_params* p,
+              double* prices, int32_t* status, cudaStream_t stream)
+{
+    const int m_pad = (m + kwg::kTile - 1) / kwg::kTile * kwg::kTile;
+    kwg::PdeBatch b;
+    b.t = (const double*)(io + L.t);
+    b.z = (const double*)(io + L.z);
+    b.r = (const double*)(io + L.r);
+    b.q = (const double*)(io + L.q);
+    b.w = (const int8_t*)(io + L.w);
+    b.e = (const uint8_t*)(io + L.e);
+    b.m = m;
+    b.m_pad = m_pad;
+    kwg::AssetBatch a;
+    a.s = (const double*)(io + L.s);
+    a.k = (const double*)(io + L.k);
+    a.pde = (const int32_t*)(io + L.pde);
+    a.n = n;
+    const kwg::Fd1dShape sh = make_shape(p);
+
+    const size_t cbytes = kwg::fd1d_fp64_coef_bytes(m_pad, sh.x_dim);
+    const size_t sbytes = kwg::fd1d_fp64_state_bytes(m_pad, sh.x_dim);
+    if (int rc = ensure_device(ctx, &ctx->d_work, &ctx->work_bytes, cbytes + sbytes)) return rc;
+    double* coef = (double*)ctx->d_work;
+    double* state = (double*)((char*)ctx->d_work + cbytes);
+    const int blocks = kwg::fd1d_fp64_solve_blocks(m_pad / kwg::kTile, ctx->device);
+    ctx->launches += kwg::fd1d_fp64_launch(b, a, sh, coef, state, (int32_t*)(io + L.pde_status), ctx->d_counter,
+                                           prices, status, blocks, stream, ctx->next_events());
+    KWG_CUDA(ctx, cudaGetLastError());
+    return KWG_OK;
+}
+
+}  // namespace
+
+
+extern "C" {
+
+void kwg_fd1d_params_default(kwg_fd1d_params* p)
+{
+    if (!p) return;
+    p->t_dim = 512;
+    p->x_dim = 512;
+    p->theta = 0.5;
+    p->scale = 50.;
+    p->density = 0.25;
+    p->precision = KWG_FP64;
+    p->solver = KWG_SOLVER_AUTO;
+    p->strict = 0;
+    p->reserved = 0;
+}
+
+kwg_ctx* kwg_create(int device)
+{
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) return nullptr;
+    if (cudaSetDevice(device) != cudaSuccess) return nullptr;
+    kwg_ctx* ctx = new kwg_ctx();
+    ctx->device = device;
+    cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&ctx->d_counter, sizeof(int)) != cudaSuccess) {
+        kwg_destroy(ctx);
+        return nullptr;
+    }
+    return ctx;
+}
+
+void kwg_destroy(kwg_ctx* ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->d_work) cudaFree(ctx->d_work);
+    if (ctx->d_io) cudaFree(ctx->d_io);
+    if (ctx->d_counter) cudaFree(ctx->d_counter);
+    if (ctx->h_io) cudaFreeHost(ctx->h_io);
+    for (auto& e : ctx->events) {
+        cudaEventDestroy(e.start);
+        cudaEventDestroy(e.stop);
+    }
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* kwg_last_error(const kwg_ctx* ctx) { return ctx ? ctx->err.c_str() : "kwg: null context"; }
+
+int kwg_last_launch_count(const kwg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int kwg_set_profiling(kwg_ctx* ctx, int enable)
+{
+    if (!ctx) return KWG_ERR_INVALID;
+    ctx->profiling = enable != 0;
+    ctx->events_used = 0;
+    return KWG_OK;
+}
+
+int kwg_profile_read(kwg_ctx* ctx, double* solve_ms, int* solve_launches)
+{
+    if (!ctx) return KWG_ERR_INVALID;
+    double total = 0.;
+    for (size_t i = 0; i < ctx->events_used; ++i) {
+        KWG_CUDA(ctx, cudaEventSynchronize(ctx->events[i].stop));
+        float ms = 0.f;
+        KWG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->events[i].start, ctx->events[i].stop));
+        total += ms;
+    }
+    if (solve_ms) *solve_ms = total;
+    if (solve_launches) *solve_launches = (int)ctx->events_used;
+    ctx->events_used = 0;
+    return KWG_OK;
+}
+
+int kwg_fd1d_price(kwg_ctx* ctx, const kwg_option* opts, size_t n, const kwg_fd1d_params* p, double* prices,
+                   int32_t* status)
+{
+    if (!ctx) return KWG_ERR_INVALID;
+    ctx->err.clear();
+    ctx->launches = 0;
+    if (int rc = check_params(ctx, p)) return rc;
+    if (n == 0) return KWG_OK;
+    if (!opts || !prices) return set_err(ctx, KWG_ERR_INVALID, "kwg: null options or prices");
+    if (n > (size_t)INT32_MAX / 2) return set_err(ctx, KWG_ERR_INVALID, "kwg: batch too large");
+    KWG_CUDA(ctx, cudaSetDevice(ctx->device));
+
+    // 1. dedup (src/Pricer/kwFd1d.cpp:28-65): sort by (t, r, q, z, e, w).
+    auto key = [&](uint32_t i) {
+        const kwg_option& o = opts[i];
+        return std::tie(o.t, o.r, o.q, o.z, o.e, o.w);
+    };
+    std::vector<uint32_t> order(n);
+    std::iota(order.begin(), order.end(), 0u);
+    std::sort(order.begin(), order.end(), [&](uint32_t l, uint32_t r) { return key(l) < key(r); });
+    std::vector<int32_t> asset2pde(n);
+    std::vector<uint32_t> pde2asset;
+    pde2asset.reserve(n);
+    pde2asset.push_back(order[0]);
+    asset2pde[order[0]] = 0;
+    for (size_t i = 1; i < n; ++i) {
+        const uint32_t l = order[i - 1], r = order[i];
+        const bool equal = (key(l) < key(r)) == (key(r) < key(l));
+        if (!equal) pde2asset.push_back(r);
+        asset2pde[r] = (int32_t)(pde2asset.size() - 1);
+    }
+    const size_t m = pde2asset.size();
+    const size_t m_pad = (m + kwg::kTile - 1) / kwg::kTile * kwg::kTile;
+
+    // 2. pack into pinned memory
+    const IoLayout L = io_layout(m, m_pad, n);
+    if (int rc = ensure_host(ctx, &ctx->h_io, &ctx->h_io_bytes, L.total)) return rc;
+    if (int rc = ensure_device(ctx, &ctx->d_io, &ctx->io_bytes, L.total)) return rc;
+    char* h = (char*)ctx->h_io;
+    double *t = (double*)(h + L.t), *z = (double*)(h + L.z), *r = (double*)(h + L.r), *q = (double*)(h + L.q);
+    int8_t* w = (int8_t*)(h + L.w);
+    uint8_t* e = (uint8_t*)(h + L.e);
+    for (size_t j = 0; j < m; ++j) {
+        const kwg_option& o = opts[pde2asset[j]];
+        t[j] = o.t;
+        z[j] = o.z;
+        r[j] = o.r;
+        q[j] = o.q;
+        w[j] = o.w;
+        e[j] = o.e;
+    }
+    double *s = (double*)(h + L.s), *k = (double*)(h + L.k);
+    int32_t* pde = (int32_t*)(h + L.pde);
+    for (size_t i = 0; i < n; ++i) {
+        s[i] = opts[i].s;
+        k[i] = opts[i].k;
+        pde[i] = asset2pde[i];
+    }
+    KWG_CUDA(ctx, cudaMemcpyAsync(ctx->d_io, ctx->h_io, L.in_bytes, cudaMemcpyHostToDevice, ctx->stream));
+
+    // 3. kernels
+    char* dio = (char*)ctx->d_io;
+    if (int rc = run_batch(ctx, dio, L, (int)m, (int)n, p, (double*)(dio + L.prices), (int32_t*)(dio + L.status),
+                           ctx->stream))
+        return rc;
+
+    // 4. results
+    KWG_CUDA(ctx, cudaMemcpyAsync(h + L.prices, (char*)ctx->d_io + L.prices, L.out_bytes, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    KWG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const double* hp = (const double*)(h + L.prices);
+    const int32_t* hs = (const int32_t*)(h + L.status);
+    std::memcpy(prices, hp, n * sizeof(double));
+    if (status) std::memcpy(status, hs, n * sizeof(int32_t));
+    if (p->strict) {
+        for (size_t i = 0; i < n; ++i) {
+            if (hs[i] == KWG_STATUS_OK) continue;
+            char msg[256];
+            if (hs[i] == KWG_STATUS_OUT_OF_GRID) {
+                std::snprintf(msg, sizeof msg, "Fd1dGpu_Pricer::price: asset %zu: x=%f not in grid range", i,
+                              std::log(opts[i].s / opts[i].k));
+                return set_err(ctx, KWG_ERR_OUT_OF_GRID, msg);
+            }
+            std::snprintf(msg, sizeof msg, "Fd1dGpu_Pricer::price: asset %zu: status %d", i, (int)hs[i]);
+            return set_err(ctx, hs[i] == KWG_STATUS_SOLVER ? KWG_ERR_SOLVER : KWG_ERR_INVALID, msg);
+        }
+    }
+    return KWG_OK;
+}
+
+int kwg_fd1d_price_device(kwg_ctx* ctx, const kwg_option* d_opts, size_t n, const kwg_fd1d_params* p,
+                          double* d_prices, int32_t* d_status, void* stream_)
+{
+    if (!ctx) return KWG_ERR_INVALID;
+    ctx->err.clear();
+    ctx->launches = 0;
+    if (int rc = check_params(ctx, p)) return rc;
+    if (n == 0) return KWG_OK;
+    if (!d_opts || !d_prices) return set_err(ctx, KWG_ERR_INVALID, "kwg: null options or prices");
+    if (n > (size_t)INT32_MAX / 2) return set_err(ctx, KWG_ERR_INVALID, "kwg: batch too large");
+    KWG_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t stream = stream_ ? (cudaStream_t)stream_ : ctx->stream;
+    const size_t m = n, m_pad = (m + kwg::kTile - 1) / kwg::kTile * kwg::kTile;
+    const IoLayout L = io_layout(m, m_pad, n);
+    if (int rc = ensure_device(ctx, &ctx->d_io, &ctx->io_bytes, L.total)) return rc;
+    char* io = (char*)ctx->d_io;
+    unpack_options<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(
+        d_opts, (int)n, (double*)(io + L.t), (double*)(io + L.z), (double*)(io + L.r), (double*)(io + L.q),
+        (double*)(io + L.s), (double*)(io + L.k), (int32_t*)(io + L.pde), (int8_t*)(io + L.w),
+        (uint8_t*)(io + L.e));
+    ctx->launches += 1;
+    return run_batch(ctx, io, L, (int)m, (int)n, p, d_prices, d_status, stream);
+}
+
+}  // extern "C"

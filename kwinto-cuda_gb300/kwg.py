@@ -1,0 +1,316 @@
+"""kwg -- Python host mirror of the reference's pricer interface over libkwg.so.
+
+The reference (gituliar/kwinto-cuda) exposes pricing as C++:
+
+    kw::Config                    typed string->value map     src/Core/kwConfig.h:21-73
+    kw::Pricer::init / price      abstract pricer             src/Pricer/kwPricer.h:12-22
+    kw::PricerFactory::create     keyed on PRICER             src/Pricer/kwPricerFactory.h:15-41
+    kw::Fd1d_Pricer               FD1D.* keys                 src/Pricer/kwFd1d.cpp:9-19
+
+This module mirrors those names, argument meanings and error behaviour (an error
+is a non-empty string; "" means success) on top of the C ABI in include/kwg.h.
+The GPU library must be built (``__graft_entry__.build()``); importing this module
+without it raises -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libkwg.so")
+
+# kw::Option layout (src/Core/kwAsset.h:12-22): t k z r q s (f64), e (u8), w (i8); 56 bytes.
+OPTION_DTYPE = np.dtype(
+    {
+        "names": ["t", "k", "z", "r", "q", "s", "e", "w"],
+        "formats": ["<f8", "<f8", "<f8", "<f8", "<f8", "<f8", "u1", "i1"],
+        "offsets": [0, 8, 16, 24, 32, 40, 48, 49],
+        "itemsize": 56,
+    }
+)
+
+KWG_OK, KWG_ERR_INVALID, KWG_ERR_CUDA, KWG_ERR_OUT_OF_GRID, KWG_ERR_SOLVER = 0, 1, 2, 3, 4
+STATUS_OK, STATUS_OUT_OF_GRID, STATUS_SOLVER, STATUS_BAD_INPUT = 0, 1, 2, 3
+FP64, FP32 = 0, 1
+SOLVER_AUTO, SOLVER_THOMAS, SOLVER_PCR = 0, 1, 2
+
+
+class Fd1dParams(ctypes.Structure):
+    """struct kwg_fd1d_params (include/kwg.h)."""
+
+    _fields_ = [
+        ("t_dim", ctypes.c_int32),
+        ("x_dim", ctypes.c_int32),
+        ("theta", ctypes.c_double),
+        ("scale", ctypes.c_double),
+        ("density", ctypes.c_double),
+        ("precision", ctypes.c_int32),
+        ("solver", ctypes.c_int32),
+        ("strict", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Loads libkwg.so once; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"kwg: {LIB_PATH} is missing; run __graft_entry__.build() first")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, sz, i32, dp = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p
+    L.kwg_fd1d_params_default.argtypes = [ctypes.POINTER(Fd1dParams)]
+    L.kwg_fd1d_params_default.restype = None
+    L.kwg_create.argtypes = [i32]
+    L.kwg_create.restype = vp
+    L.kwg_destroy.argtypes = [vp]
+    L.kwg_destroy.restype = None
+    L.kwg_last_error.argtypes = [vp]
+    L.kwg_last_error.restype = ctypes.c_char_p
+    L.kwg_last_launch_count.argtypes = [vp]
+    L.kwg_last_launch_count.restype = i32
+    L.kwg_fd1d_price.argtypes = [vp, vp, sz, ctypes.POINTER(Fd1dParams), dp, dp]
+    L.kwg_fd1d_price.restype = i32
+    L.kwg_fd1d_price_device.argtypes = [vp, vp, sz, ctypes.POINTER(Fd1dParams), dp, dp, vp]
+    L.kwg_fd1d_price_device.restype = i32
+    L.kwg_set_profiling.argtypes = [vp, i32]
+    L.kwg_set_profiling.restype = i32
+    L.kwg_profile_read.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
+    L.kwg_profile_read.restype = i32
+    _lib = L
+    return L
+
+
+def default_params() -> Fd1dParams:
+    p = Fd1dParams()
+    lib().kwg_fd1d_params_default(ctypes.byref(p))
+    return p
+
+
+class Context:
+    """Owns a kwg_ctx (device buffers + stream) on one CUDA device."""
+
+    def __init__(self, device: int = 0):
+        self._L = lib()
+        self.ptr = self._L.kwg_create(device)
+        if not self.ptr:
+            raise RuntimeError(f"kwg_create({device}) failed: no usable CUDA device")
+
+    def close(self):
+        if self.ptr:
+            self._L.kwg_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def last_error(self) -> str:
+        return self._L.kwg_last_error(self.ptr).decode()
+
+    def launch_count(self) -> int:
+        return self._L.kwg_last_launch_count(self.ptr)
+
+    def set_profiling(self, on: bool):
+        self._L.kwg_set_profiling(self.ptr, 1 if on else 0)
+
+    def profile_read(self):
+        """(summed solve-kernel ms, launches) since the last read."""
+        ms, cnt = ctypes.c_double(0), ctypes.c_int(0)
+        rc = self._L.kwg_profile_read(self.ptr, ctypes.byref(ms), ctypes.byref(cnt))
+        if rc:
+            raise RuntimeError(self.last_error())
+        return ms.value, cnt.value
+
+    def fd1d_price(self, opts: np.ndarray, params: Fd1dParams):
+        """Host arrays in, host arrays out. Returns (rc, prices, status)."""
+        opts = np.ascontiguousarray(opts, dtype=OPTION_DTYPE)
+        n = len(opts)
+        prices = np.empty(n, np.float64)
+        status = np.empty(n, np.int32)
+        rc = self._L.kwg_fd1d_price(
+            self.ptr, opts.ctypes.data, n, ctypes.byref(params), prices.ctypes.data, status.ctypes.data
+        )
+        return rc, prices, status
+
+    def fd1d_price_device(self, d_opts: int, n: int, params: Fd1dParams, d_prices: int, d_status: int,
+                          stream: int = 0) -> int:
+        """Device pointers in and out (e.g. torch tensors' data_ptr()); asynchronous."""
+        return self._L.kwg_fd1d_price_device(self.ptr, d_opts, n, ctypes.byref(params), d_prices, d_status,
+                                             stream or None)
+
+
+# ----------------------------------------------------------------------------- kw::Config
+
+
+class Config:
+    """kw::Config (src/Core/kwConfig.h:21-73): separate double / integer / string maps;
+    ``get`` looks in the map matching the type of its default."""
+
+    def __init__(self):
+        self._d: dict[str, float] = {}
+        self._i: dict[str, int] = {}
+        self._s: dict[str, str] = {}
+
+    def set(self, key: str, value):
+        if isinstance(value, bool) or isinstance(value, (int, np.integer)):
+            self._i[key] = int(value)
+        elif isinstance(value, (float, np.floating)):
+            self._d[key] = float(value)
+        elif isinstance(value, str):
+            self._s[key] = value
+        else:
+            raise TypeError(f"Config.set: unsupported type {type(value).__name__}")
+
+    def get(self, key: str, default):
+        if isinstance(default, bool) or isinstance(default, (int, np.integer)):
+            return self._i.get(key, int(default))
+        if isinstance(default, (float, np.floating)):
+            return self._d.get(key, float(default))
+        if isinstance(default, str):
+            return self._s.get(key, default)
+        raise TypeError(f"Config.get: unsupported default type {type(default).__name__}")
+
+    def erase(self, key: str):
+        for m in (self._d, self._i, self._s):
+            m.pop(key, None)
+
+
+# ----------------------------------------------------------------------------- kw::Pricer
+
+
+@dataclass
+class Option:
+    """kw::Option (src/Core/kwAsset.h:12-22)."""
+
+    t: float
+    k: float
+    z: float
+    r: float
+    q: float
+    s: float
+    e: int
+    w: int
+
+
+def to_array(assets) -> np.ndarray:
+    """List of Option (or tuples in kw::Option field order) -> OPTION_DTYPE array."""
+    if isinstance(assets, np.ndarray) and assets.dtype == OPTION_DTYPE:
+        return assets
+    out = np.zeros(len(assets), OPTION_DTYPE)
+    for i, a in enumerate(assets):
+        if isinstance(a, Option):
+            a = (a.t, a.k, a.z, a.r, a.q, a.s, a.e, a.w)
+        out[i] = tuple(a)
+    return out
+
+
+class Pricer:
+    """kw::Pricer (src/Pricer/kwPricer.h:12-22). Errors are strings, "" = success."""
+
+    def init(self, config: Config) -> str:  # pragma: no cover - interface
+        raise NotImplementedError
+
+    def price(self, assets, prices: list) -> str:  # pragma: no cover - interface
+        raise NotImplementedError
+
+
+_PRECISIONS = {"FP64": FP64, "FP32": FP32}
+_SOLVERS = {"AUTO": SOLVER_AUTO, "THOMAS": SOLVER_THOMAS, "PCR": SOLVER_PCR}
+
+
+class Fd1dGpuPricer(Pricer):
+    """Drop-in for kw::Fd1d_Pricer (src/Pricer/kwFd1d.cpp:9-160) on the GPU.
+
+    Reads the reference keys FD1D.DENSITY (0.25), FD1D.SCALE (50.),
+    FD1D.T_GRID_SIZE (512), FD1D.X_GRID_SIZE (512) with the reference defaults,
+    plus FD1D.THETA (0.5), FD1D.PRECISION ("FP64"|"FP32"), FD1D.SOLVER
+    ("AUTO"|"THOMAS"|"PCR"), FD1D.STRICT (1: fail the whole call on the first
+    out-of-grid asset like the reference, src/Pricer/kwFd1d.cpp:154-155; 0: NaN and a
+    per-option status), FD1D.DEVICE (0)."""
+
+    def __init__(self):
+        self.params = default_params()
+        self.ctx: Context | None = None
+        self.status = np.zeros(0, np.int32)
+
+    def init(self, config: Config) -> str:
+        p = self.params
+        p.density = config.get("FD1D.DENSITY", 0.25)
+        p.scale = config.get("FD1D.SCALE", 50.0)
+        p.t_dim = config.get("FD1D.T_GRID_SIZE", 512)
+        p.x_dim = config.get("FD1D.X_GRID_SIZE", 512)
+        p.theta = config.get("FD1D.THETA", 0.5)
+        prec = config.get("FD1D.PRECISION", "FP64")
+        solver = config.get("FD1D.SOLVER", "AUTO")
+        if prec not in _PRECISIONS:
+            return f"Fd1dGpu_Pricer::init: unknown FD1D.PRECISION = {prec}"
+        if solver not in _SOLVERS:
+            return f"Fd1dGpu_Pricer::init: unknown FD1D.SOLVER = {solver}"
+        p.precision = _PRECISIONS[prec]
+        p.solver = _SOLVERS[solver]
+        p.strict = config.get("FD1D.STRICT", 1)
+        try:
+            self.ctx = Context(config.get("FD1D.DEVICE", 0))
+        except RuntimeError as ex:
+            return f"Fd1dGpu_Pricer::init: {ex}"
+        return ""
+
+    def price(self, assets, prices: list) -> str:
+        arr = to_array(assets)
+        if len(arr) == 0:
+            return ""
+        if self.ctx is None:
+            return "Fd1dGpu_Pricer::price: init was not called"
+        rc, out, status = self.ctx.fd1d_price(arr, self.params)
+        self.status = status
+        prices[:] = out.tolist()
+        if rc != KWG_OK:
+            return "Fd1dGpu_Pricer::price: " + self.ctx.last_error()
+        return ""
+
+    def price_array(self, arr: np.ndarray):
+        """Fast path: OPTION_DTYPE array -> (error, prices ndarray, status ndarray)."""
+        rc, out, status = self.ctx.fd1d_price(arr, self.params)
+        return ("" if rc == KWG_OK else "Fd1dGpu_Pricer::price: " + self.ctx.last_error()), out, status
+
+
+class PricerFactory:
+    """kw::PricerFactory (src/Pricer/kwPricerFactory.h:15-41).  "FD1D" and "FD1D-GPU"
+    both create the GPU FD pricer (the drop-in); unknown keys are an error."""
+
+    @staticmethod
+    def create(config: Config):
+        mode = config.get("PRICER", "")
+        if not mode:
+            return "PricerFactory: Missing PRICER key", None
+        if mode in ("FD1D", "FD1D-GPU"):
+            pricer = Fd1dGpuPricer()
+        else:
+            return f"PricerFactory: Unknown PRICER = {mode}", None
+        err = pricer.init(config)
+        if err:
+            return "PricerFactory: " + err, None
+        return "", pricer
+
+
+def params(t_dim=512, x_dim=512, theta=0.5, scale=50.0, density=0.25, precision=FP64, solver=SOLVER_AUTO,
+           strict=0) -> Fd1dParams:
+    p = default_params()
+    p.t_dim, p.x_dim, p.theta, p.scale, p.density = t_dim, x_dim, theta, scale, density
+    p.precision, p.solver, p.strict = precision, solver, strict
+    return p
+
+
+UNIFORM = math.inf  # density value selecting the uniform grid

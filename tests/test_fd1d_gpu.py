@@ -1,0 +1,195 @@
+"""GPU parity of the FP64 FD1D path against the oracle and the reference's golden
+vectors, through the C ABI.  Tolerance: the FP64 path must match the reference to
+REL_TOL = 1e-10 relative on every option."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-10
+
+
+def rel_err(got, want):
+    return float(np.max(np.abs(got - want) / np.abs(want)))
+
+
+def gpu_price(ctx, opts, **kw):
+    import kwg
+
+    rc, p, st = ctx.fd1d_price(opts, kwg.params(**kw))
+    assert rc == kwg.KWG_OK, ctx.last_error()
+    return p, st
+
+
+def test_pricer_test_table(ctx):
+    """test/kwPricer_test.cpp:63-84 at the reference defaults (512x512, scale 50, d 0.25)."""
+    g = golden("pricer_test.npz")
+    p, st = gpu_price(ctx, g["opts"])
+    assert (st == 0).all()
+    assert rel_err(p, g["ref_fd1d"]) <= REL_TOL
+    assert np.max(np.abs(p - g["want"])) <= 1.3e-3
+
+
+@pytest.mark.parametrize("name", ["qdfp", "fd1d"])
+def test_portfolio_fixtures(ctx, name):
+    """test/kwPortfolio_test.cpp:41-56: 6000 puts, 600 distinct PDEs (dedup path)."""
+    g = golden(f"portfolio_{name}.npz")
+    p, st = gpu_price(ctx, g["opts"], t_dim=512, x_dim=512)
+    assert (st == 0).all()
+    assert rel_err(p, g["ref_fd1d"]) <= REL_TOL
+    if name == "qdfp":
+        assert np.max(np.abs(p - g["quantlib"])) <= 0.005
+
+
+def test_config1(ctx):
+    g = golden("synthetic.npz")
+    p, st = gpu_price(ctx, g["config1_opts"], t_dim=512, x_dim=512, scale=5.0, density=0.25)
+    assert (st == 0).all() and rel_err(p, g["config1_ref"]) <= REL_TOL
+
+
+def test_config2_sample_sinh_and_uniform(ctx):
+    """1024x1024: the reference at density 1e6, the GPU both at 1e6 and exactly uniform."""
+    g = golden("synthetic.npz")
+    p, _ = gpu_price(ctx, g["config2_opts"], t_dim=1024, x_dim=1024, scale=5.0, density=1e6)
+    assert rel_err(p, g["config2_ref"]) <= REL_TOL
+    u, _ = gpu_price(ctx, g["config2_opts"], t_dim=1024, x_dim=1024, scale=5.0, density=math.inf)
+    assert rel_err(u, g["config2_ref"]) <= REL_TOL
+
+
+def test_config4_sample(ctx):
+    g = golden("synthetic.npz")
+    p, _ = gpu_price(ctx, g["config4_opts"], t_dim=2048, x_dim=2048, scale=5.0, density=0.25)
+    assert rel_err(p, g["config4_ref"]) <= REL_TOL
+
+
+@pytest.mark.parametrize("name,kw", [("default", {}), ("x3_t2", dict(x_dim=3, t_dim=2)),
+                                     ("x7_t5", dict(x_dim=7, t_dim=5)),
+                                     ("x64_t33", dict(x_dim=64, t_dim=33, scale=5.0))])
+def test_edge_grids_european_calls_duplicates(ctx, name, kw):
+    g = golden("edge.npz")
+    p, st = gpu_price(ctx, g["opts"], **kw)
+    assert (st == 0).all() and rel_err(p, g[f"ref_{name}"]) <= REL_TOL
+
+
+def test_out_of_grid_status_and_strict(ctx):
+    import kwg
+
+    g = golden("edge.npz")
+    p, st = gpu_price(ctx, g["bad_opts"])
+    assert st[3] == kwg.STATUS_OUT_OF_GRID and np.isnan(p[3])
+    ok = np.arange(8) != 3
+    assert (st[ok] == 0).all() and rel_err(p[ok], g["ref_default"][ok]) <= REL_TOL
+    rc, _, _ = ctx.fd1d_price(g["bad_opts"], kwg.params(strict=1))
+    assert rc == kwg.KWG_ERR_OUT_OF_GRID and "not in grid range" in ctx.last_error()
+
+
+@pytest.mark.parametrize("theta", [0.6, 0.75, 1.0])
+def test_theta_other_than_half(ctx, theta):
+    """theta is hard-coded to 0.5 in the reference; other values follow the oracle."""
+    import kwor
+
+    o = golden("synthetic.npz")["config1_opts"][:40]
+    p, _ = gpu_price(ctx, o, t_dim=200, x_dim=160, scale=5.0, density=0.25, theta=theta)
+    rc, msg, want, _ = kwor.fd1d_price(o, t_dim=200, x_dim=160, scale=5.0, density=0.25, theta=theta)
+    assert rc == 0, msg
+    assert rel_err(p, want) <= REL_TOL
+
+
+@pytest.mark.parametrize("n", [1, 31, 33, 100])
+def test_ragged_batches(ctx, n):
+    """PDE counts that are not a multiple of the 32-lane tile."""
+    import kwor
+    import portfolio
+
+    o = portfolio.config1_like(n, seed=99)
+    p, st = gpu_price(ctx, o, t_dim=64, x_dim=96, scale=5.0, density=0.25)
+    rc, msg, want, _ = kwor.fd1d_price(o, t_dim=64, x_dim=96, scale=5.0, density=0.25)
+    assert (st == 0).all() and rel_err(p, want) <= REL_TOL
+
+
+def test_empty_batch_and_invalid_params(ctx):
+    import kwg
+
+    rc, p, st = ctx.fd1d_price(np.zeros(0, kwg.OPTION_DTYPE), kwg.params())
+    assert rc == kwg.KWG_OK and len(p) == 0
+    o = golden("edge.npz")["opts"]
+    for bad in (dict(x_dim=2), dict(t_dim=1), dict(theta=0.0), dict(theta=1.5), dict(scale=-1.0),
+                dict(density=0.0)):
+        rc, _, _ = ctx.fd1d_price(o, kwg.params(**bad))
+        assert rc == kwg.KWG_ERR_INVALID, bad
+        assert ctx.last_error().startswith("kwg:")
+
+
+def test_bad_option_fields(ctx):
+    import kwg
+
+    o = golden("edge.npz")["opts"].copy()
+    o[1]["t"] = 0.0
+    o[5]["z"] = -0.2
+    o[7]["s"] = 0.0
+    p, st = gpu_price(ctx, o)
+    assert st[1] == kwg.STATUS_BAD_INPUT and st[5] == kwg.STATUS_BAD_INPUT and st[7] == kwg.STATUS_BAD_INPUT
+    assert np.isnan(p[[1, 5, 7]]).all()
+    assert (st[[0, 2, 3, 4, 6]] == 0).all()
+
+
+def test_device_api_matches_host_api(ctx):
+    import torch
+
+    import kwg
+    import portfolio
+
+    o = portfolio.config1_like(300, seed=5)
+    prm = kwg.params(t_dim=128, x_dim=256, scale=5.0, density=0.25)
+    want, _ = gpu_price(ctx, o, t_dim=128, x_dim=256, scale=5.0, density=0.25)
+    d_o = torch.from_numpy(o.view(np.uint8).copy()).cuda()
+    d_p = torch.empty(len(o), dtype=torch.float64, device="cuda")
+    d_s = torch.empty(len(o), dtype=torch.int32, device="cuda")
+    rc = ctx.fd1d_price_device(d_o.data_ptr(), len(o), prm, d_p.data_ptr(), d_s.data_ptr(),
+                               torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, ctx.last_error()
+    torch.cuda.synchronize()
+    assert np.array_equal(d_p.cpu().numpy(), want)
+    assert (d_s.cpu().numpy() == 0).all()
+
+
+def test_pricer_mirror(built):
+    """kw::PricerFactory / kw::Pricer usage exactly like test/kwPricer_test.cpp:63-84."""
+    import kwg
+
+    g = golden("pricer_test.npz")
+    assets = [kwg.Option(*[float(x) for x in tuple(r)[:6]], int(r["e"]), int(r["w"])) for r in g["opts"]]
+    config = kwg.Config()
+    config.set("PRICER", "FD1D")
+    err, pricer = kwg.PricerFactory.create(config)
+    assert err == ""
+    prices = []
+    assert pricer.price(assets, prices) == ""
+    for want, got in zip(g["want"], prices):
+        assert abs(want - got) <= 1.3e-3
+    bad = golden("edge.npz")["bad_opts"]
+    err = pricer.price(bad, prices)
+    assert err.startswith("Fd1dGpu_Pricer::price:") and "not in grid range" in err
+
+
+def test_config2_full_size_properties(ctx):
+    """All 32768 options at 1024x1024: finite, American >= intrinsic (the projection
+    floors every node and the payoff is convex), deterministic, and a sample equal to
+    the oracle."""
+    import kwor
+    import portfolio
+
+    o = portfolio.config1_like(32768, seed=42)
+    p, st = gpu_price(ctx, o, t_dim=1024, x_dim=1024, scale=5.0, density=math.inf)
+    assert (st == 0).all() and np.isfinite(p).all()
+    intrinsic = np.where(o["w"] < 0, np.maximum(o["k"] - o["s"], 0), np.maximum(o["s"] - o["k"], 0))
+    assert (p >= intrinsic - 1e-9).all()
+    p2, _ = gpu_price(ctx, o, t_dim=1024, x_dim=1024, scale=5.0, density=math.inf)
+    assert np.array_equal(p, p2)
+    idx = np.arange(0, 32768, 1024)
+    rc, msg, want, _ = kwor.fd1d_price(o[idx], t_dim=1024, x_dim=1024, scale=5.0, density=math.inf)
+    assert rc == 0 and rel_err(p[idx], want) <= REL_TOL

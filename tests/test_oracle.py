@@ -1,0 +1,125 @@
+"""Pins the oracle (C restatement of the reference, oracle/fd1d_oracle.c) against the
+reference's own golden vectors and, where it is built, the reference itself.  CPU only."""
+import numpy as np
+import pytest
+
+from conftest import golden
+
+
+@pytest.fixture(scope="module")
+def kwor(built):
+    import kwor as m
+
+    return m
+
+
+def test_pricer_test_table_fd1d(kwor):
+    """test/kwPricer_test.cpp:63-84: FD1D at reference defaults within 1.3e-3."""
+    g = golden("pricer_test.npz")
+    rc, msg, p, st = kwor.fd1d_price(g["opts"])
+    assert rc == 0, msg
+    assert np.max(np.abs(p - g["want"])) <= 1.3e-3
+    assert np.array_equal(p, g["ref_fd1d"]), "oracle must reproduce the reference bit for bit"
+
+
+def test_pricer_test_table_bs(kwor):
+    """test/kwPricer_test.cpp:37-60: Black-Scholes skips American (NaN) options."""
+    g = golden("pricer_test.npz")
+    p = kwor.bs_price(g["opts"])
+    euro = g["opts"]["e"] == 0
+    assert np.all(np.isnan(p[~euro]))
+    assert np.max(np.abs(p[euro] - g["want"][euro])) <= 1.3e-3
+    assert np.array_equal(p[euro], g["ref_bs"][euro])
+
+
+def test_pricer_test_table_fd1d_bs(kwor):
+    """test/kwPricer_test.cpp:87-107: FD1D-BS control variate within 1.3e-3."""
+    g = golden("pricer_test.npz")
+    rc, msg, p, _ = kwor.fd1d_price(g["opts"], bs=True)
+    assert rc == 0, msg
+    assert np.max(np.abs(p - g["want"])) <= 1.3e-3
+    assert np.array_equal(p, g["ref_fd1d_bs"])
+
+
+@pytest.mark.parametrize("name", ["qdfp", "fd1d"])
+def test_portfolio_fixtures(kwor, name):
+    """test/kwPortfolio_test.cpp:41-56 (qdfp within 0.005 of QuantLib); bitwise vs ref."""
+    g = golden(f"portfolio_{name}.npz")
+    rc, msg, p, _ = kwor.fd1d_price(g["opts"], t_dim=512, x_dim=512)
+    assert rc == 0, msg
+    assert np.array_equal(p, g["ref_fd1d"])
+    if name == "qdfp":
+        assert np.max(np.abs(p - g["quantlib"])) <= 0.005
+
+
+def test_synthetic_workloads(kwor):
+    g = golden("synthetic.npz")
+    rc, msg, p, _ = kwor.fd1d_price(g["config1_opts"], t_dim=512, x_dim=512, scale=5.0, density=0.25)
+    assert rc == 0 and np.array_equal(p, g["config1_ref"])
+    rc, msg, p, _ = kwor.fd1d_price(g["config2_opts"][:64], t_dim=1024, x_dim=1024, scale=5.0, density=1e6)
+    assert rc == 0 and np.array_equal(p, g["config2_ref"][:64])
+    rc, msg, p, _ = kwor.fd1d_price(g["config4_opts"][:4], t_dim=2048, x_dim=2048, scale=5.0, density=0.25)
+    assert rc == 0 and np.array_equal(p, g["config4_ref"][:4])
+
+
+def test_edge_cases(kwor):
+    g = golden("edge.npz")
+    for name, kw in {"default": {}, "x3_t2": dict(x_dim=3, t_dim=2), "x7_t5": dict(x_dim=7, t_dim=5),
+                     "x64_t33": dict(x_dim=64, t_dim=33, scale=5.0)}.items():
+        rc, msg, p, _ = kwor.fd1d_price(g["opts"], **kw)
+        assert rc == 0, msg
+        assert np.array_equal(p, g[f"ref_{name}"]), name
+    rc, msg, p, st = kwor.fd1d_price(g["bad_opts"])
+    assert rc == kwor.OUT_OF_GRID and "not in range" in msg
+    assert st[3] == kwor.OUT_OF_GRID and np.isnan(p[3])
+    assert (st[np.arange(8) != 3] == 0).all()
+
+
+def test_dedup_shares_pde(kwor):
+    """Options differing only in s/k share one PDE (src/Pricer/kwFd1d.cpp:28-65): pricing
+    them together or one by one gives identical prices."""
+    g = golden("edge.npz")
+    o = g["opts"]
+    rc, _, together, _ = kwor.fd1d_price(o)
+    alone = np.array([kwor.fd1d_price(o[i:i + 1])[2][0] for i in range(len(o))])
+    assert np.array_equal(together, alone)
+
+
+def test_const_dt_and_uniform_are_close(kwor):
+    """The GPU uses dt = T/(tDim-1) on every step and an exactly uniform grid for
+    density=inf; both stay far inside the 1e-10 parity bar."""
+    g = golden("synthetic.npz")
+    o = g["config1_opts"][:32]
+    _, _, a, _ = kwor.fd1d_price(o, t_dim=512, x_dim=512, scale=5.0, density=0.25)
+    _, _, b, _ = kwor.fd1d_price(o, t_dim=512, x_dim=512, scale=5.0, density=0.25, const_dt=True)
+    assert np.max(np.abs(a - b) / a) < 1e-11
+    o2 = g["config2_opts"][:16]
+    _, _, c, _ = kwor.fd1d_price(o2, t_dim=256, x_dim=256, scale=5.0, density=1e6)
+    _, _, d, _ = kwor.fd1d_price(o2, t_dim=256, x_dim=256, scale=5.0, density=float("inf"))
+    assert np.max(np.abs(c - d) / c) < 1e-10
+
+
+def test_theta_one_is_implicit_euler(kwor):
+    """theta=1 must reduce to B V' = V (E = identity)."""
+    o = golden("edge.npz")["opts"][:2]
+    rc, _, p, _ = kwor.fd1d_price(o, theta=1.0, x_dim=64, t_dim=16)
+    assert rc == 0 and np.all(np.isfinite(p))
+
+
+def test_reference_matches_oracle_live(kwor):
+    """Where the reference is built here, re-run it and the oracle on a fresh sample."""
+    if not kwor.ref_available():
+        pytest.skip("reference library not built here")
+    import portfolio
+
+    o = portfolio.config1_like(48, seed=1234)
+    runs = [kwor.ref_price(o, density=0.25, scale=5.0, t_dim=200, x_dim=300) for _ in range(2)]
+    if not np.array_equal(runs[0][2], runs[1][2]):
+        # the reference pool's wait() can return before the last job ends
+        # (src/kwThreadPool.cpp:58-72); a third run settles which one was torn
+        runs.append(kwor.ref_price(o, density=0.25, scale=5.0, t_dim=200, x_dim=300))
+        runs = [runs[2]]
+    rc, msg, want, _ = runs[0]
+    assert rc == 0, msg
+    rc, msg, got, _ = kwor.fd1d_price(o, t_dim=200, x_dim=300, scale=5.0, density=0.25)
+    assert np.array_equal(got, want)
