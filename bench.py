@@ -48,8 +48,8 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 
 
-def node_steps(n, x_dim=X_DIM, t_dim=T_DIM):
-    return n * x_dim * (t_dim - 1)
+def node_steps(n, x_dim=None, t_dim=None):
+    return n * (x_dim or X_DIM) * ((t_dim or T_DIM) - 1)
 
 
 # Algorithmic traffic of the FP64 streaming solve per node and step: V and the sweep
@@ -216,7 +216,9 @@ def run_ours(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     ctx = kwg.Context(local)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated non-default stream: the kernels and the timing events share it
+    # (a NULL stream handle would mean the context's own stream to the C ABI)
+    stream = torch.cuda.Stream(dev)
 
     # each rank prices its own batch (weak scaling), drawn from its own window of the stream
     opts = portfolio.config1_like(N_OPTIONS, seed=42, start=rank * N_OPTIONS)
@@ -356,8 +358,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--options", type=int, default=N_OPTIONS,
                     help="options per batch (default 32768; smaller values are for profiling captures)")
+    ap.add_argument("--t-dim", type=int, default=T_DIM,
+                    help="time steps (default 1024; shorter runs are for profiling captures)")
     args = ap.parse_args()
     globals()["N_OPTIONS"] = args.options
+    globals()["T_DIM"] = args.t_dim
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -38,6 +38,7 @@ extern "C" {
 #define KWG_STATUS_OUT_OF_GRID 1 /* price is NaN; the reference fails the whole batch here */
 #define KWG_STATUS_SOLVER 2      /* price is NaN; zero/non-finite pivot in the factorisation */
 #define KWG_STATUS_BAD_INPUT 3   /* price is NaN; t<=0, z<=0, k<=0 or s<=0 */
+#define KWG_STATUS_DEVICE_TIMEOUT 4 /* price is NaN; a bounded device-side wait expired */
 
 /* ---- numeric modes ------------------------------------------------------------------- */
 #define KWG_FP64 0 /* all stepping in FP64: parity with the reference to <= 1e-10 relative */

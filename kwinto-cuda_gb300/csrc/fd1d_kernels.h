@@ -42,8 +42,8 @@ struct Fd1dShape {
     bool uniform;
 };
 
-size_t fd1d_fp64_coef_bytes(int m_pad, int x_dim);
-size_t fd1d_fp64_state_bytes(int m_pad, int x_dim);
+// Device bytes of the node records of a batch (coefficients + state).
+size_t fd1d_fp64_work_bytes(int m_pad, int x_dim);
 
 // Optional CUDA events recorded immediately before and after the solve kernel.
 struct SolveEvents {
@@ -51,9 +51,10 @@ struct SolveEvents {
 };
 
 // Launches setup, solve and interpolation on `stream`; returns the launch count.
-int fd1d_fp64_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* coef, double* state,
-                     int32_t* pde_status, int* tile_counter, double* prices, int32_t* status, int solve_blocks,
-                     cudaStream_t stream, const SolveEvents* ev);
+// counters: 2 ints, [0] tile queue, [1] device-timeout flag (zeroed here).
+int fd1d_fp64_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* rec, int32_t* pde_status,
+                     int* counters, double* prices, int32_t* status, int solve_blocks, cudaStream_t stream,
+                     const SolveEvents* ev);
 
 // Occupancy-derived persistent grid size for the FP64 solve kernel.
 int fd1d_fp64_solve_blocks(int ntiles, int device);

@@ -34,7 +34,7 @@ struct kwg_ctx {
     size_t work_bytes = 0;
     void* d_io = nullptr;  // packed inputs / outputs
     size_t io_bytes = 0;
-    int* d_counter = nullptr;
+    int* d_counter = nullptr;  // [0] tile queue, [1] device-timeout flag
     // pinned host staging
     void* h_io = nullptr;
     size_t h_io_bytes = 0;
@@ -206,14 +206,11 @@ int run_batch(kwg_ctx* ctx, char* io, const IoLayout& L, int m, int n, const kwg
     a.n = n;
     const kwg::Fd1dShape sh = make_shape(p);
 
-    const size_t cbytes = kwg::fd1d_fp64_coef_bytes(m_pad, sh.x_dim);
-    const size_t sbytes = kwg::fd1d_fp64_state_bytes(m_pad, sh.x_dim);
-    if (int rc = ensure_device(ctx, &ctx->d_work, &ctx->work_bytes, cbytes + sbytes)) return rc;
-    double* coef = (double*)ctx->d_work;
-    double* state = (double*)((char*)ctx->d_work + cbytes);
+    const size_t wbytes = kwg::fd1d_fp64_work_bytes(m_pad, sh.x_dim);
+    if (int rc = ensure_device(ctx, &ctx->d_work, &ctx->work_bytes, wbytes)) return rc;
     const int blocks = kwg::fd1d_fp64_solve_blocks(m_pad / kwg::kTile, ctx->device);
-    ctx->launches += kwg::fd1d_fp64_launch(b, a, sh, coef, state, (int32_t*)(io + L.pde_status), ctx->d_counter,
-                                           prices, status, blocks, stream, ctx->next_events());
+    ctx->launches += kwg::fd1d_fp64_launch(b, a, sh, (double*)ctx->d_work, (int32_t*)(io + L.pde_status),
+                                           ctx->d_counter, prices, status, blocks, stream, ctx->next_events());
     KWG_CUDA(ctx, cudaGetLastError());
     return KWG_OK;
 }
@@ -246,7 +243,7 @@ kwg_ctx* kwg_create(int device)
     ctx->device = device;
     cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMalloc(&ctx->d_counter, sizeof(int)) != cudaSuccess) {
+        cudaMalloc(&ctx->d_counter, 2 * sizeof(int)) != cudaSuccess) {
         kwg_destroy(ctx);
         return nullptr;
     }

@@ -11,10 +11,12 @@ from conftest import golden
 pytestmark = pytest.mark.gpu
 
 REL_TOL = 1e-10
+# prices below this are compared absolutely (a reference price can be exactly 0)
+PRICE_FLOOR = 1e-12
 
 
 def rel_err(got, want):
-    return float(np.max(np.abs(got - want) / np.abs(want)))
+    return float(np.max(np.abs(got - want) / np.maximum(np.abs(want), PRICE_FLOOR)))
 
 
 def gpu_price(ctx, opts, **kw):
@@ -177,9 +179,11 @@ def test_pricer_mirror(built):
 
 
 def test_config2_full_size_properties(ctx):
-    """All 32768 options at 1024x1024: finite, American >= intrinsic (the projection
-    floors every node and the payoff is convex), deterministic, and a sample equal to
-    the oracle."""
+    """All 32768 options at 1024x1024: finite, American >= intrinsic up to the
+    interpolation error of the payoff, deterministic, and a sample equal to the oracle.
+    The projection floors every node but the last at the payoff; between nodes the
+    price is a chord, which for a put ((1 - e^x)+, concave where positive) lies below
+    the payoff by at most K dx^2/8, as it does in the reference."""
     import kwor
     import portfolio
 
@@ -187,7 +191,8 @@ def test_config2_full_size_properties(ctx):
     p, st = gpu_price(ctx, o, t_dim=1024, x_dim=1024, scale=5.0, density=math.inf)
     assert (st == 0).all() and np.isfinite(p).all()
     intrinsic = np.where(o["w"] < 0, np.maximum(o["k"] - o["s"], 0), np.maximum(o["s"] - o["k"], 0))
-    assert (p >= intrinsic - 1e-9).all()
+    dx = 2 * 5.0 * o["z"] * np.sqrt(o["t"]) / (1024 - 1)
+    assert (p >= intrinsic - 1.01 * o["k"] * dx * dx / 8 - 1e-9).all()
     p2, _ = gpu_price(ctx, o, t_dim=1024, x_dim=1024, scale=5.0, density=math.inf)
     assert np.array_equal(p, p2)
     idx = np.arange(0, 32768, 1024)
