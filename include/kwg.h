@@ -109,6 +109,23 @@ int kwg_fd1d_price_device(kwg_ctx* ctx, const kwg_option* d_opts, size_t n,
                           const kwg_fd1d_params* p, double* d_prices, int32_t* d_status,
                           void* stream);
 
+/* No counterpart in the reference.  The FP64 device call for callers that cannot
+ * allocate device memory -- for example a pricing step inside a host application
+ * whose device memory belongs to another allocator or is held to a fixed budget, or
+ * a latency-critical path where cudaMalloc's implicit synchronisation is not allowed.
+ * Same computation and results as kwg_fd1d_price_device, but it needs no context and
+ * allocates nothing: all scratch is one 64 MiB __device__ array inside the library
+ * (about 80 bytes per option and grid node: roughly 800 options at x_dim 1024), held
+ * by every GPU that loads the library until the process exits.  Larger batches are
+ * rejected with KWG_ERR_INVALID and a message.  The first call on a device looks up
+ * the array's address with that device current; make it before any stream capture.
+ * Calls share the array: calls that overlap on the GPU race, so serialise them.
+ * `stream` is a cudaStream_t (NULL = the legacy default stream); `err` (may be NULL)
+ * receives the error message.  Asynchronous like kwg_fd1d_price_device. */
+int kwg_fd1d_price_device_static(const kwg_option* d_opts, size_t n, const kwg_fd1d_params* p,
+                                 double* d_prices, int32_t* d_status, void* stream, char* err,
+                                 size_t errlen);
+
 /* Number of kernel launches the last pricing call made (for launch accounting). */
 int kwg_last_launch_count(const kwg_ctx* ctx);
 
