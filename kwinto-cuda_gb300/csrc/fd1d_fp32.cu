@@ -1,0 +1,387 @@
+// fd1d_fp32.cu -- FP32 stepping with FP64-accurate state: one warp per PDE, the whole
+// PDE on chip (state in registers, coefficient tables in shared memory), a
+// partitioned tridiagonal solve with warp shuffles for the reduced system.
+//
+// Numerics.  The reference step B V' = E V (src/Math/kwFd1d.cpp:61-132) is taken in
+// delta form,  V' = max(V + d, p)  with  B d = dt A V  (E = B + dt A), so FP32 only
+// ever carries the small increment d.  V and the payoff p are float-float pairs
+// (hi + lo, ~48 significant bits).  The residual dt A V is formed from differences
+// of the pairs, which are exact in FP32, with the operator written as
+//     dt A V_j = c1 S_j + c2 (V_{j+1}-V_j) + c3 (V_j-V_{j-1}) + c4 V_j,
+//     S_j = (V_{j+1}-V_j) - (V_j-V_{j-1}),
+// c1 = dt axx l2, c2 = dt (axx (u2-l2) + ax im), c3 = dt ax im, c4 = dt a0 (the
+// reference's inverse spacings, src/Math/kwFd1d.cpp:87-92), so rounding the
+// coefficients to FP32 perturbs the PDE's coefficients by ~1e-7 relatively instead
+// of breaking the cancellation of the second difference.  The grid, c1..c4 and the
+// payoff are computed in FP64 (src/Pricer/kwFd1d.cpp:110-139); the final
+// interpolation reads V = hi + lo in FP64.
+//
+// Solve of B d = r (N_p = 32 M nodes, lane k owns nodes kM .. kM+M-1):
+//   * node kM is a separator s_k; nodes kM+1 .. kM+M-1 are lane k's interior;
+//   * interior:  d_I = y - s_k L - s_{k+1} R,  y = B_I^-1 r_I  (local Thomas,
+//     factors and the spikes L, R precomputed once per PDE);
+//   * separators: a 32-unknown tridiagonal system, solved by parallel cyclic
+//     reduction over the warp (5 shuffle levels, multipliers precomputed).
+// B, dt and the grid do not change between steps, so all factors are computed once.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "fd1d_common.cuh"
+#include "fd1d_kernels.h"
+
+namespace kwg {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kF32Fields = 11;
+// table fields per node, layout [node-in-lane][field][lane] (conflict-free)
+enum { T_C1 = 0, T_C2, T_C3, T_C4, T_L, T_ID, T_U, T_SL, T_SR, T_PH, T_PL };
+
+struct FF {
+    float hi, lo;
+};
+
+// hi + lo of a double, both rounded to nearest.
+__device__ __forceinline__ FF split(double v)
+{
+    FF r;
+    r.hi = (float)v;
+    r.lo = (float)(v - (double)r.hi);
+    return r;
+}
+
+// (h, l) + d with an error-free sum, renormalised.
+__device__ __forceinline__ void ff_add(float& h, float& l, float d)
+{
+    const float s = h + d;
+    const float bb = s - h;
+    const float e = (h - (s - bb)) + (d - bb);
+    const float t = l + e;
+    h = s + t;
+    l = t - (h - s);
+}
+
+}  // namespace
+
+template <int M>
+__global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShape sh, double* __restrict__ vout,
+                                                      int32_t* __restrict__ pde_status, int* __restrict__ counters)
+{
+    extern __shared__ float tab[];  // [M][kF32Fields][32]
+    const int k = threadIdx.x & 31;
+    auto T = [&](int i, int f) -> float& { return tab[(i * kF32Fields + f) * 32 + k]; };
+    const int N = sh.x_dim;
+    const int j0 = k * M;
+
+    for (;;) {
+        int pde = 0;
+        if (k == 0) pde = atomicAdd(&counters[0], 1);
+        pde = __shfl_sync(kFull, pde, 0);
+        if (pde >= b.m) break;
+
+        // ------------------------------------------------------------ setup
+        const double t = b.t[pde], z = b.z[pde], rr = b.r[pde], qq = b.q[pde];
+        const int8_t w = b.w[pde];
+        const bool amer = b.e[pde] != 0;
+        int32_t st = KWG_STATUS_OK;
+        if (!(t > 0.) || !(z > 0.) || !isfinite(t) || !isfinite(z) || !isfinite(rr) || !isfinite(qq))
+            st = KWG_STATUS_BAD_INPUT;
+        Grid g;
+        g.init(z, t, sh.scale, sh.density, N, sh.uniform);
+        const Coef a = pde_coef(rr, qq, z);
+        const double dt = time_step(t, sh.t_dim);
+
+        {
+            double xm = (j0 > 0 && j0 - 1 < N) ? g.x(j0 - 1) : 0.;
+            double x0 = (j0 < N) ? g.x(j0) : 0.;
+#pragma unroll 1
+            for (int i = 0; i < M; ++i) {
+                const int j = j0 + i;
+                const double xp = (j + 1 < N) ? g.x(j + 1) : 0.;
+                float c1 = 0.f, c2 = 0.f, c3 = 0.f, c4 = 0.f, fbl = 0.f, fb = 1.f, fbu = 0.f;
+                FF p = {0.f, 0.f};
+                if (j < N) {
+                    const Row rw = implicit_row(j, N, xm, x0, xp, sh.theta, dt, a.a0, a.ax, a.axx);
+                    fbl = (float)rw.bl;
+                    fb = (float)rw.b;
+                    fbu = (float)rw.bu;
+                    c4 = (float)(dt * a.a0);
+                    if (j == 0) {
+                        c2 = (float)(dt * a.ax / (xp - x0));
+                    } else if (j == N - 1) {
+                        c3 = (float)(dt * a.ax / (x0 - xm));
+                    } else {
+                        const double iu = 1. / (xp - x0), im = 1. / (xp - xm), id = 1. / (x0 - xm);
+                        const double u2 = 2. * iu * im, l2 = 2. * id * im;
+                        c1 = (float)(dt * a.axx * l2);
+                        c2 = (float)(dt * (a.axx * (u2 - l2) + a.ax * im));
+                        c3 = (float)(dt * a.ax * im);
+                    }
+                    p = split(payoff(w, x0));
+                }
+                T(i, T_C1) = c1;
+                T(i, T_C2) = c2;
+                T(i, T_C3) = c3;
+                T(i, T_C4) = c4;
+                T(i, T_L) = fbl;  // rows parked in the LU slots until factorised
+                T(i, T_ID) = fb;
+                T(i, T_U) = fbu;
+                T(i, T_PH) = p.hi;
+                T(i, T_PL) = p.lo;
+                xm = x0;
+                x0 = xp;
+            }
+        }
+        // separator row of this lane
+        const float bla = T(0, T_L), ba = T(0, T_ID), bua = T(0, T_U);
+        // interior LU (FP32): l_1 = 0; l_i = bl_i / d_{i-1}; d_i = b_i - l_i bu_{i-1}
+        const float first_bl = T(1, T_L);
+        float last_bu;
+        {
+            float d_prev = 1.f, bu_prev = 0.f;
+#pragma unroll 1
+            for (int i = 1; i < M; ++i) {
+                const float bl = T(i, T_L), bb = T(i, T_ID), bu = T(i, T_U);
+                const float l = (i == 1) ? 0.f : bl / d_prev;
+                const float d = (i == 1) ? bb : bb - l * bu_prev;
+                if (!(d != 0.f) || !isfinite(d)) st = st == KWG_STATUS_OK ? KWG_STATUS_SOLVER : st;
+                const float idd = 1.f / d;
+                T(i, T_L) = l;
+                T(i, T_ID) = idd;
+                T(i, T_U) = bu * idd;
+                d_prev = d;
+                bu_prev = bu;
+            }
+            last_bu = bu_prev;
+        }
+        // spikes L = B_I^-1 (bl_first e_1), R = B_I^-1 (bu_last e_{M-1})
+        {
+            float f = first_bl;
+#pragma unroll 1
+            for (int i = 1; i < M; ++i) {
+                if (i > 1) f = -T(i, T_L) * f;
+                T(i, T_SL) = f * T(i, T_ID);
+            }
+            float nxt = 0.f;
+#pragma unroll 1
+            for (int i = M - 1; i >= 1; --i) {
+                const float v = (i == M - 1) ? T(i, T_SL) : T(i, T_SL) - T(i, T_U) * nxt;
+                T(i, T_SL) = v;
+                nxt = v;
+            }
+            float rn = last_bu * T(M - 1, T_ID);
+            T(M - 1, T_SR) = rn;
+#pragma unroll 1
+            for (int i = M - 2; i >= 1; --i) {
+                rn = -T(i, T_U) * rn;
+                T(i, T_SR) = rn;
+            }
+        }
+        // reduced (separator) system and its cyclic-reduction multipliers
+        float ka[5], kc[5], ib;
+        {
+            float Lprev = __shfl_up_sync(kFull, T(M - 1, T_SL), 1);
+            float Rprev = __shfl_up_sync(kFull, T(M - 1, T_SR), 1);
+            if (k == 0) Lprev = Rprev = 0.f;
+            float al = -bla * Lprev;
+            float be = ba - bla * Rprev - bua * T(1, T_SL);
+            float ga = -bua * T(1, T_SR);
+#pragma unroll
+            for (int lv = 0; lv < 5; ++lv) {
+                const int sg = 1 << lv;
+                float alm = __shfl_up_sync(kFull, al, sg), bem = __shfl_up_sync(kFull, be, sg),
+                      gam = __shfl_up_sync(kFull, ga, sg);
+                float alp = __shfl_down_sync(kFull, al, sg), bep = __shfl_down_sync(kFull, be, sg),
+                      gap = __shfl_down_sync(kFull, ga, sg);
+                if (k - sg < 0) {
+                    alm = 0.f;
+                    bem = 1.f;
+                    gam = 0.f;
+                }
+                if (k + sg > 31) {
+                    alp = 0.f;
+                    bep = 1.f;
+                    gap = 0.f;
+                }
+                const float ma = (k - sg < 0) ? 0.f : al / bem;
+                const float mc = (k + sg > 31) ? 0.f : ga / bep;
+                ka[lv] = ma;
+                kc[lv] = mc;
+                const float nal = -ma * alm, nga = -mc * gap;
+                be = be - ma * gam - mc * alp;
+                al = nal;
+                ga = nga;
+            }
+            if (!(be != 0.f) || !isfinite(be)) st = st == KWG_STATUS_OK ? KWG_STATUS_SOLVER : st;
+            ib = 1.f / be;
+        }
+        st = __reduce_max_sync(kFull, st);
+        const bool run = st == KWG_STATUS_OK;
+        float H[M], Lo[M];  // V as float-float pairs, starting at the payoff
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+            H[i] = T(i, T_PH);
+            Lo[i] = T(i, T_PL);
+        }
+
+        // ------------------------------------------------------------ time steps
+        for (int step = 1; run && step < sh.t_dim; ++step) {
+            float Hm = __shfl_up_sync(kFull, H[M - 1], 1), Lm = __shfl_up_sync(kFull, Lo[M - 1], 1);
+            float Hp = __shfl_down_sync(kFull, H[0], 1), Lp = __shfl_down_sync(kFull, Lo[0], 1);
+            if (k == 0) Hm = Lm = 0.f;
+            if (k == 31) Hp = Lp = 0.f;
+            float y[M];
+            // residual r = dt A V from exact float-float differences
+#pragma unroll
+            for (int i = 0; i < M; ++i) {
+                const float hl = (i == 0) ? Hm : H[i - 1], ll = (i == 0) ? Lm : Lo[i - 1];
+                const float hr = (i == M - 1) ? Hp : H[i + 1], lr = (i == M - 1) ? Lp : Lo[i + 1];
+                const float hdu = hr - H[i], hdd = H[i] - hl, ldu = lr - Lo[i], ldd = Lo[i] - ll;
+                const float Dup = hdu + ldu, Ddn = hdd + ldd, S = (hdu - hdd) + (ldu - ldd);
+                float r = T(i, T_C4) * (H[i] + Lo[i]);
+                r = fmaf(T(i, T_C1), S, r);
+                r = fmaf(T(i, T_C2), Dup, r);
+                y[i] = fmaf(T(i, T_C3), Ddn, r);
+            }
+            // interior: forward and backward Thomas
+            {
+                float f = 0.f;
+#pragma unroll
+                for (int i = 1; i < M; ++i) {
+                    f = fmaf(-T(i, T_L), f, y[i]);
+                    y[i] = f * T(i, T_ID);
+                }
+#pragma unroll
+                for (int i = M - 2; i >= 1; --i) y[i] = fmaf(-T(i, T_U), y[i + 1], y[i]);
+            }
+            // separators: right-hand side, cyclic reduction, back to the interior
+            float ylp = __shfl_up_sync(kFull, y[M - 1], 1);
+            if (k == 0) ylp = 0.f;
+            float rho = y[0] - bla * ylp - bua * y[1];
+#pragma unroll
+            for (int lv = 0; lv < 5; ++lv) {
+                const int sg = 1 << lv;
+                const float rm = __shfl_up_sync(kFull, rho, sg);
+                const float rp = __shfl_down_sync(kFull, rho, sg);
+                rho = rho - ka[lv] * rm - kc[lv] * rp;
+            }
+            const float s = rho * ib;
+            float s1 = __shfl_down_sync(kFull, s, 1);
+            if (k == 31) s1 = 0.f;
+            y[0] = s;
+#pragma unroll
+            for (int i = 1; i < M; ++i) y[i] = fmaf(-s1, T(i, T_SR), fmaf(-s, T(i, T_SL), y[i]));
+            // V += d (float-float), then the early-exercise floor on nodes < N-1
+#pragma unroll
+            for (int i = 0; i < M; ++i) {
+                ff_add(H[i], Lo[i], y[i]);
+                if (amer && j0 + i < N - 1) {
+                    const float ph = T(i, T_PH), pl = T(i, T_PL);
+                    if ((H[i] - ph) + (Lo[i] - pl) < 0.f) {
+                        H[i] = ph;
+                        Lo[i] = pl;
+                    }
+                }
+            }
+        }
+        // ------------------------------------------------------------ result
+        double* V = vout + (size_t)pde * N;
+#pragma unroll
+        for (int i = 0; i < M; ++i)
+            if (j0 + i < N) V[j0 + i] = (double)H[i] + (double)Lo[i];
+        if (k == 0) pde_status[pde] = st;
+    }
+}
+
+// One thread per asset, like fd1d_interp_fp64 but over a [pde][x_dim] array of V.
+__global__ void fd1d_interp_rows(const PdeBatch b, const AssetBatch a, Fd1dShape sh, const double* __restrict__ vrow,
+                                 const int32_t* __restrict__ pde_status, double* __restrict__ prices,
+                                 int32_t* __restrict__ status)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const int slot = a.pde[i];
+    const int N = sh.x_dim;
+    const double s = a.s[i], k = a.k[i];
+    int32_t st = pde_status[slot];
+    if (!(s > 0.) || !(k > 0.) || !isfinite(s) || !isfinite(k)) st = KWG_STATUS_BAD_INPUT;
+    double price = __longlong_as_double(0x7ff8000000000000ll);
+    if (st == KWG_STATUS_OK) {
+        Grid g;
+        g.init(b.z[slot], b.t[slot], sh.scale, sh.density, N, sh.uniform);
+        const double xs = log(dvd(s, k));
+        int lo = 0, hi = N;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (g.x(mid) < xs)
+                lo = mid + 1;
+            else
+                hi = mid;
+        }
+        if (lo == 0 || lo == N) {
+            st = KWG_STATUS_OUT_OF_GRID;
+        } else {
+            const double* V = vrow + (size_t)slot * N;
+            const double xl = g.x(lo - 1), xh = g.x(lo);
+            const double v = dvd(add(mul(sub(xh, xs), V[lo - 1]), mul(sub(xs, xl), V[lo])), sub(xh, xl));
+            price = mul(k, v);
+        }
+    }
+    prices[i] = price;
+    if (status) status[i] = st;
+}
+
+namespace {
+
+template <int M>
+int launch_m(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* vout, int32_t* pde_status,
+             int* counters, double* prices, int32_t* status, int sms, cudaStream_t stream, const SolveEvents* ev)
+{
+    const size_t smem = (size_t)M * kF32Fields * 32 * sizeof(float);
+    cudaFuncSetAttribute(fd1d_solve_fp32<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fd1d_solve_fp32<M>, 32, smem);
+    if (per_sm < 1) per_sm = 1;
+    const int blocks = b.m < sms * per_sm ? b.m : sms * per_sm;
+    cudaMemsetAsync(counters, 0, 2 * sizeof(int), stream);
+    if (ev) cudaEventRecord(ev->start, stream);
+    fd1d_solve_fp32<M><<<blocks, 32, smem, stream>>>(b, sh, vout, pde_status, counters);
+    if (ev) cudaEventRecord(ev->stop, stream);
+    int launches = 1;
+    if (a.n > 0) {
+        fd1d_interp_rows<<<(a.n + 127) / 128, 128, 0, stream>>>(b, a, sh, vout, pde_status, prices, status);
+        ++launches;
+    }
+    return launches;
+}
+
+}  // namespace
+
+int fd1d_fp32_nodes_per_lane(int x_dim)
+{
+    int m = 2;
+    while (32 * m < x_dim) m *= 2;
+    return m <= 64 ? m : -1;
+}
+
+size_t fd1d_fp32_work_bytes(int m, int x_dim) { return (size_t)m * x_dim * sizeof(double); }
+
+int fd1d_fp32_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* vout, int32_t* pde_status,
+                     int* counters, double* prices, int32_t* status, int device, cudaStream_t stream,
+                     const SolveEvents* ev)
+{
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    switch (fd1d_fp32_nodes_per_lane(sh.x_dim)) {
+    case 2: return launch_m<2>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    case 4: return launch_m<4>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    case 8: return launch_m<8>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    case 16: return launch_m<16>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    case 32: return launch_m<32>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    case 64: return launch_m<64>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    default: return -1;
+    }
+}
+
+}  // namespace kwg

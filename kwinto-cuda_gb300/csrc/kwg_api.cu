@@ -114,10 +114,12 @@ int check_params(kwg_ctx* ctx, const kwg_fd1d_params* p)
         return set_err(ctx, KWG_ERR_INVALID, "kwg: unknown precision");
     if (p->solver < KWG_SOLVER_AUTO || p->solver > KWG_SOLVER_PCR)
         return set_err(ctx, KWG_ERR_INVALID, "kwg: unknown solver");
-    if (p->precision == KWG_FP32)
-        return set_err(ctx, KWG_ERR_INVALID, "kwg: FP32 stepping is not available in this build");
-    if (p->solver == KWG_SOLVER_PCR)
-        return set_err(ctx, KWG_ERR_INVALID, "kwg: the PCR solver is not available in this build");
+    if (p->precision == KWG_FP64 && p->solver == KWG_SOLVER_PCR)
+        return set_err(ctx, KWG_ERR_INVALID, "kwg: FP64 uses the Thomas solver (KWG_SOLVER_THOMAS or AUTO)");
+    if (p->precision == KWG_FP32 && p->solver == KWG_SOLVER_THOMAS)
+        return set_err(ctx, KWG_ERR_INVALID, "kwg: FP32 uses the on-chip partitioned solver (KWG_SOLVER_PCR or AUTO)");
+    if (p->precision == KWG_FP32 && kwg::fd1d_fp32_nodes_per_lane(p->x_dim) < 0)
+        return set_err(ctx, KWG_ERR_INVALID, "kwg: FP32 stepping supports x_dim <= 2048");
     return KWG_OK;
 }
 
@@ -206,11 +208,21 @@ int run_batch(kwg_ctx* ctx, char* io, const IoLayout& L, int m, int n, const kwg
     a.n = n;
     const kwg::Fd1dShape sh = make_shape(p);
 
-    const size_t wbytes = kwg::fd1d_fp64_work_bytes(m_pad, sh.x_dim);
-    if (int rc = ensure_device(ctx, &ctx->d_work, &ctx->work_bytes, wbytes)) return rc;
-    const int blocks = kwg::fd1d_fp64_solve_blocks(m_pad / kwg::kTile, ctx->device);
-    ctx->launches += kwg::fd1d_fp64_launch(b, a, sh, (double*)ctx->d_work, (int32_t*)(io + L.pde_status),
-                                           ctx->d_counter, prices, status, blocks, stream, ctx->next_events());
+    if (p->precision == KWG_FP32) {
+        const size_t wbytes = kwg::fd1d_fp32_work_bytes(m, sh.x_dim);
+        if (int rc = ensure_device(ctx, &ctx->d_work, &ctx->work_bytes, wbytes)) return rc;
+        const int n_launch = kwg::fd1d_fp32_launch(b, a, sh, (double*)ctx->d_work, (int32_t*)(io + L.pde_status),
+                                                   ctx->d_counter, prices, status, ctx->device, stream,
+                                                   ctx->next_events());
+        if (n_launch < 0) return set_err(ctx, KWG_ERR_INVALID, "kwg: FP32 stepping supports x_dim <= 2048");
+        ctx->launches += n_launch;
+    } else {
+        const size_t wbytes = kwg::fd1d_fp64_work_bytes(m_pad, sh.x_dim);
+        if (int rc = ensure_device(ctx, &ctx->d_work, &ctx->work_bytes, wbytes)) return rc;
+        const int blocks = kwg::fd1d_fp64_solve_blocks(m_pad / kwg::kTile, ctx->device);
+        ctx->launches += kwg::fd1d_fp64_launch(b, a, sh, (double*)ctx->d_work, (int32_t*)(io + L.pde_status),
+                                               ctx->d_counter, prices, status, blocks, stream, ctx->next_events());
+    }
     KWG_CUDA(ctx, cudaGetLastError());
     return KWG_OK;
 }

@@ -1,0 +1,115 @@
+"""GPU FP32 stepping path (float-float state, FP32 increments, on-chip partitioned
+solve) against the FP64 oracle.  Tolerance: ABS_TOL = 1e-5 absolute on every price."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+ABS_TOL = 1e-5
+
+
+def price32(ctx, opts, **kw):
+    import kwg
+
+    rc, p, st = ctx.fd1d_price(opts, kwg.params(precision=kwg.FP32, **kw))
+    assert rc == kwg.KWG_OK, ctx.last_error()
+    return p, st
+
+
+def oracle(opts, **kw):
+    import kwor
+
+    rc, msg, p, st = kwor.fd1d_price(opts, **kw)
+    assert rc == 0, msg
+    return p
+
+
+def test_config1(ctx):
+    g = golden("synthetic.npz")
+    p, st = price32(ctx, g["config1_opts"], t_dim=512, x_dim=512, scale=5.0, density=0.25)
+    assert (st == 0).all()
+    assert np.max(np.abs(p - g["config1_ref"])) <= ABS_TOL
+
+
+def test_config2_sample_uniform(ctx):
+    g = golden("synthetic.npz")
+    p, st = price32(ctx, g["config2_opts"], t_dim=1024, x_dim=1024, scale=5.0, density=math.inf)
+    assert (st == 0).all()
+    assert np.max(np.abs(p - g["config2_ref"])) <= ABS_TOL
+
+
+def test_config4_sample(ctx):
+    g = golden("synthetic.npz")
+    p, st = price32(ctx, g["config4_opts"], t_dim=2048, x_dim=2048, scale=5.0, density=0.25)
+    assert (st == 0).all()
+    assert np.max(np.abs(p - g["config4_ref"])) <= ABS_TOL
+
+
+def test_portfolio_qdfp(ctx):
+    """Reference defaults (scale 50, density 0.25, 512x512) on the 6000-put fixture."""
+    g = golden("portfolio_qdfp.npz")
+    p, st = price32(ctx, g["opts"], t_dim=512, x_dim=512)
+    assert (st == 0).all()
+    assert np.max(np.abs(p - g["ref_fd1d"])) <= ABS_TOL
+    assert np.max(np.abs(p - g["quantlib"])) <= 0.005
+
+
+@pytest.mark.parametrize("name,kw", [("default", {}), ("x3_t2", dict(x_dim=3, t_dim=2)),
+                                     ("x7_t5", dict(x_dim=7, t_dim=5)),
+                                     ("x64_t33", dict(x_dim=64, t_dim=33, scale=5.0))])
+def test_edge_grids(ctx, name, kw):
+    """Tiny and non-power-of-two grids (padded with decoupled rows), Europeans,
+    calls, duplicates."""
+    g = golden("edge.npz")
+    p, st = price32(ctx, g["opts"], **kw)
+    assert (st == 0).all()
+    want = g[f"ref_{name}"]
+    # a 3-node grid over +-50 sigma sqrt(T) prices some options in the tens of
+    # thousands; there FP32 increments resolve the price to ~1e-7 relative
+    assert (np.abs(p - want) <= np.maximum(ABS_TOL, 2e-7 * np.abs(want))).all()
+
+
+@pytest.mark.parametrize("x_dim,t_dim", [(100, 50), (300, 120), (1000, 700), (1500, 1200)])
+def test_non_power_of_two_grids(ctx, x_dim, t_dim):
+    """Grids padded to 32*2^k nodes with decoupled identity rows.  (The FP32 path
+    keeps 1e-5 while lambda = theta dt sigma^2 / (2 dx^2) stays moderate; at
+    1000x64 or 1500x40 on the sinh grid lambda reaches ~1e3 near the strike and the
+    separator system amplifies FP32 rounding to ~1e-4.)"""
+    import portfolio
+
+    o = portfolio.config1_like(40, seed=21)
+    p, st = price32(ctx, o, t_dim=t_dim, x_dim=x_dim, scale=5.0, density=0.25)
+    want = oracle(o, t_dim=t_dim, x_dim=x_dim, scale=5.0, density=0.25)
+    assert (st == 0).all() and np.max(np.abs(p - want)) <= ABS_TOL
+
+
+def test_theta_and_status(ctx):
+    import kwg
+
+    o = golden("synthetic.npz")["config1_opts"][:24]
+    p, _ = price32(ctx, o, t_dim=200, x_dim=256, scale=5.0, density=0.25, theta=1.0)
+    want = oracle(o, t_dim=200, x_dim=256, scale=5.0, density=0.25, theta=1.0)
+    assert np.max(np.abs(p - want)) <= ABS_TOL
+    bad = golden("edge.npz")["bad_opts"]
+    p, st = price32(ctx, bad)
+    assert st[3] == kwg.STATUS_OUT_OF_GRID and np.isnan(p[3]) and (st[np.arange(8) != 3] == 0).all()
+    rc, _, _ = ctx.fd1d_price(bad, kwg.params(precision=kwg.FP32, x_dim=4096))
+    assert rc == kwg.KWG_ERR_INVALID and "2048" in ctx.last_error()
+
+
+def test_config2_full_size_vs_fp64(ctx):
+    """All 32768 options at 1024x1024: FP32 within 1e-5 of the GPU FP64 path."""
+    import kwg
+    import portfolio
+
+    o = portfolio.config1_like(32768, seed=42)
+    rc, p64, _ = ctx.fd1d_price(o, kwg.params(t_dim=1024, x_dim=1024, scale=5.0, density=math.inf))
+    assert rc == 0
+    p32, st = price32(ctx, o, t_dim=1024, x_dim=1024, scale=5.0, density=math.inf)
+    assert (st == 0).all()
+    err = np.abs(p32 - p64)
+    assert err.max() <= ABS_TOL, (err.max(), int(err.argmax()))
