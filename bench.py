@@ -142,6 +142,25 @@ def cpu_oracle_rate(opts_all, budget_s=12.0):
         n = min(len(opts_all), int(n * max(2.0, budget_s / 4 / max(dt, 1e-3))))
 
 
+def fp64_peak_tflops(dev):
+    """FP64 peak of this GPU, measured as cuBLAS DGEMM 4096^3 (best of 5)."""
+    import torch
+
+    a = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    b = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize(dev)
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        best = max(best, 2 * 4096**3 / (e0.elapsed_time(e1) / 1e3) / 1e12)
+    return best
+
+
 def fp64_error_sample(opts, gpu_prices, k=64):
     """Max relative error of GPU FP64 prices against the oracle on an evenly spaced sample."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -227,8 +246,8 @@ def run_ours(args):
     d_prices = torch.empty(N_OPTIONS, dtype=torch.float64, device=dev)
     d_status = torch.empty(N_OPTIONS, dtype=torch.int32, device=dev)
 
-    def step():
-        rc = ctx.fd1d_price_device(d_opts.data_ptr(), N_OPTIONS, prm, d_prices.data_ptr(), d_status.data_ptr(),
+    def step(params=prm):
+        rc = ctx.fd1d_price_device(d_opts.data_ptr(), N_OPTIONS, params, d_prices.data_ptr(), d_status.data_ptr(),
                                    stream.cuda_stream)
         if rc != 0:
             raise RuntimeError(ctx.last_error())
@@ -291,10 +310,32 @@ def run_ours(args):
     h2d = N_OPTIONS * (4 * 8 + 2) + N_OPTIONS * (2 * 8 + 4)
     d2h = N_OPTIONS * (8 + 4)
 
+    # ---------------------------------------------------------------- FP32 variant (resident)
+    prm32 = kwg.params(t_dim=T_DIM, x_dim=X_DIM, scale=SCALE, density=DENSITY, precision=kwg.FP32)
+    for _ in range(args.warmup):
+        step(prm32)
+    barrier()
+    ctx.set_profiling(True)
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(args.steps):
+        launches32 = step(prm32)
+    f1.record(stream)
+    barrier()
+    solve32_ms, solve32_n = ctx.profile_read()
+    ctx.set_profiling(False)
+    ms32 = max_over_ranks(f0.elapsed_time(f1))
+    value32 = ws * N_OPTIONS * args.steps / (ms32 / 1e3)
+    p32 = d_prices.cpu().numpy()
+    if not (d_status.cpu().numpy() == 0).all():
+        raise RuntimeError("FP32: options failed")
+    err32 = np.abs(p32 - gpu_prices)
+
     if ws > 1:
         torch.distributed.destroy_process_group()
     if rank != 0:
         return
+    fp64_peak = fp64_peak_tflops(dev)
 
     # ---------------------------------------------------------------- roofline (solve kernel)
     hbm, peak_src = peaks()
@@ -338,12 +379,20 @@ def run_ours(args):
                      "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_src, "traffic": traffic,
                      "algorithmic_bytes_per_node_step": FP64_BYTES_PER_NODE_STEP,
                      "node_steps_per_launch": ns, "launch_ms": per_launch_s * 1e3,
-                     "fp64_tflops": fp64_tflops},
+                     "fp64_tflops": fp64_tflops, "fp64_peak_tflops": fp64_peak,
+                     "fp64_frac": fp64_tflops / fp64_peak if fp64_peak else None,
+                     "fp64_peak_source": "measured here: cuBLAS DGEMM 4096^3"},
         "cpu_baseline": ({"value": cpu_rate, "unit": "options/s", "cores": cpu_threads, "kind": "port",
                           "sample": f"{cpu_n} options of the batch at 1024x1024 ({cpu_s:.1f} s), oracle C "
                                     f"restatement, {cpu_threads} threads"} if cpu_rate else None),
         "variants": {"fd64": {"options_per_sec": value, "max_rel_err_vs_oracle": err,
-                              "oracle_sample": nerr}},
+                              "oracle_sample": nerr},
+                     "fd32": {"options_per_sec": value32, "ms_per_step": ms32 / args.steps,
+                              "solve_ms": solve32_ms / max(solve32_n, 1),
+                              "speedup_vs_fd64": value32 / value,
+                              "max_abs_err_vs_fd64": float(err32.max()),
+                              "p99_abs_err_vs_fd64": float(np.percentile(err32, 99)),
+                              "gpu_launches_per_step": launches32}},
     }
     print(json.dumps(line), flush=True)
 

@@ -92,20 +92,31 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
         const Coef a = pde_coef(rr, qq, z);
         const double dt = time_step(t, sh.t_dim);
 
+        // One FP64 pass over this lane's nodes: grid, operator row, residual
+        // coefficients, payoff, and the LU of the interior block B_I with the four
+        // spike end values the separator system needs (L_1, L_{M-1}, R_1, R_{M-1}).
+        // The separator system nearly cancels when theta dt sigma^2/dx^2 is large, so
+        // its coefficients come from FP64; the per-step arrays are stored in FP32.
+        double bla = 0., ba = 1., bua = 0.;          // separator row (node kM)
+        double L1 = 0., Llast = 0., R1 = 0., Rlast = 0.;
+        double bl_first_f = 0., bu_last_f = 0.;   // first interior bl, last interior bu
         {
             double xm = (j0 > 0 && j0 - 1 < N) ? g.x(j0 - 1) : 0.;
             double x0 = (j0 < N) ? g.x(j0) : 0.;
+            double d_prev = 1., id_prev = 1., bu_prev = 0.;
+            double pu = 1., pl = 1., sum = 0., fL = 0., bl_first = 0., pr = 1.;
 #pragma unroll 1
             for (int i = 0; i < M; ++i) {
                 const int j = j0 + i;
                 const double xp = (j + 1 < N) ? g.x(j + 1) : 0.;
-                float c1 = 0.f, c2 = 0.f, c3 = 0.f, c4 = 0.f, fbl = 0.f, fb = 1.f, fbu = 0.f;
+                double bl = 0., bb = 1., bu = 0.;
+                float c1 = 0.f, c2 = 0.f, c3 = 0.f, c4 = 0.f;
                 FF p = {0.f, 0.f};
                 if (j < N) {
                     const Row rw = implicit_row(j, N, xm, x0, xp, sh.theta, dt, a.a0, a.ax, a.axx);
-                    fbl = (float)rw.bl;
-                    fb = (float)rw.b;
-                    fbu = (float)rw.bu;
+                    bl = rw.bl;
+                    bb = rw.b;
+                    bu = rw.bu;
                     c4 = (float)(dt * a.a0);
                     if (j == 0) {
                         c2 = (float)(dt * a.ax / (xp - x0));
@@ -118,46 +129,61 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
                         c2 = (float)(dt * (a.axx * (u2 - l2) + a.ax * im));
                         c3 = (float)(dt * a.ax * im);
                     }
-                    p = split(payoff(w, x0));
+                    // the payoff is exactly 0 on the out-of-the-money side: skip exp there
+                    if ((w < 0) ? (x0 < 0.) : (x0 > 0.)) p = split(payoff(w, x0));
                 }
                 T(i, T_C1) = c1;
                 T(i, T_C2) = c2;
                 T(i, T_C3) = c3;
                 T(i, T_C4) = c4;
-                T(i, T_L) = fbl;  // rows parked in the LU slots until factorised
-                T(i, T_ID) = fb;
-                T(i, T_U) = fbu;
                 T(i, T_PH) = p.hi;
                 T(i, T_PL) = p.lo;
+                if (i == 0) {
+                    bla = bl;
+                    ba = bb;
+                    bua = bu;
+                } else {
+                    // LU of B_I: l_1 = 0, d_1 = b_1; l_i = bl_i/d_{i-1}, d_i = b_i - l_i bu_{i-1}
+                    const double l = (i == 1) ? 0. : bl * id_prev;
+                    const double d = (i == 1) ? bb : bb - l * bu_prev;
+                    if (!(d != 0.) || !isfinite(d)) st = st == KWG_STATUS_OK ? KWG_STATUS_SOLVER : st;
+                    const double idd = 1. / d;
+                    const double u = bu * idd;
+                    T(i, T_L) = (float)l;
+                    T(i, T_ID) = (float)idd;
+                    T(i, T_U) = (float)u;
+                    // spike ends: L = B_I^-1 (bl_1 e_1), R = B_I^-1 (bu_{M-1} e_{M-1}).
+                    // L_1 = bl_1 (B_I^-1)_11 = bl_1 sum_k prod_{i<k}(-u_i) / d_k prod_{2<=i<=k}(-l_i)
+                    if (i == 1) {
+                        bl_first = bl;
+                        fL = bl;
+                    } else {
+                        pl *= -l;
+                        fL *= -l;
+                    }
+                    sum += pu * idd * pl;
+                    if (i == M - 1) {
+                        pr = pu;  // prod_{1<=i<=M-2} (-u_i)
+                        Llast = fL * idd;
+                        Rlast = bu * idd;
+                        bu_last_f = bu;
+                    }
+                    pu *= -u;
+                    d_prev = d;
+                    id_prev = idd;
+                }
+                bu_prev = bu;
                 xm = x0;
                 x0 = xp;
             }
+            (void)d_prev;
+            L1 = bl_first * sum;
+            R1 = Rlast * pr;
+            bl_first_f = bl_first;
         }
-        // separator row of this lane
-        const float bla = T(0, T_L), ba = T(0, T_ID), bua = T(0, T_U);
-        // interior LU (FP32): l_1 = 0; l_i = bl_i / d_{i-1}; d_i = b_i - l_i bu_{i-1}
-        const float first_bl = T(1, T_L);
-        float last_bu;
+        // full spike arrays for the per-step correction, in FP32 from the stored LU
         {
-            float d_prev = 1.f, bu_prev = 0.f;
-#pragma unroll 1
-            for (int i = 1; i < M; ++i) {
-                const float bl = T(i, T_L), bb = T(i, T_ID), bu = T(i, T_U);
-                const float l = (i == 1) ? 0.f : bl / d_prev;
-                const float d = (i == 1) ? bb : bb - l * bu_prev;
-                if (!(d != 0.f) || !isfinite(d)) st = st == KWG_STATUS_OK ? KWG_STATUS_SOLVER : st;
-                const float idd = 1.f / d;
-                T(i, T_L) = l;
-                T(i, T_ID) = idd;
-                T(i, T_U) = bu * idd;
-                d_prev = d;
-                bu_prev = bu;
-            }
-            last_bu = bu_prev;
-        }
-        // spikes L = B_I^-1 (bl_first e_1), R = B_I^-1 (bu_last e_{M-1})
-        {
-            float f = first_bl;
+            float f = (float)bl_first_f;
 #pragma unroll 1
             for (int i = 1; i < M; ++i) {
                 if (i > 1) f = -T(i, T_L) * f;
@@ -170,7 +196,7 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
                 T(i, T_SL) = v;
                 nxt = v;
             }
-            float rn = last_bu * T(M - 1, T_ID);
+            float rn = (float)bu_last_f * T(M - 1, T_ID);
             T(M - 1, T_SR) = rn;
 #pragma unroll 1
             for (int i = M - 2; i >= 1; --i) {
@@ -178,44 +204,45 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
                 T(i, T_SR) = rn;
             }
         }
-        // reduced (separator) system and its cyclic-reduction multipliers
+        // separator system (FP64) and its cyclic-reduction multipliers (stored FP32)
         float ka[5], kc[5], ib;
         {
-            float Lprev = __shfl_up_sync(kFull, T(M - 1, T_SL), 1);
-            float Rprev = __shfl_up_sync(kFull, T(M - 1, T_SR), 1);
-            if (k == 0) Lprev = Rprev = 0.f;
-            float al = -bla * Lprev;
-            float be = ba - bla * Rprev - bua * T(1, T_SL);
-            float ga = -bua * T(1, T_SR);
+            double Lprev = __shfl_up_sync(kFull, Llast, 1);
+            double Rprev = __shfl_up_sync(kFull, Rlast, 1);
+            if (k == 0) Lprev = Rprev = 0.;
+            double al = -bla * Lprev;
+            double be = ba - bla * Rprev - bua * L1;
+            double ga = -bua * R1;
 #pragma unroll
             for (int lv = 0; lv < 5; ++lv) {
                 const int sg = 1 << lv;
-                float alm = __shfl_up_sync(kFull, al, sg), bem = __shfl_up_sync(kFull, be, sg),
-                      gam = __shfl_up_sync(kFull, ga, sg);
-                float alp = __shfl_down_sync(kFull, al, sg), bep = __shfl_down_sync(kFull, be, sg),
-                      gap = __shfl_down_sync(kFull, ga, sg);
+                double alm = __shfl_up_sync(kFull, al, sg), bem = __shfl_up_sync(kFull, be, sg),
+                       gam = __shfl_up_sync(kFull, ga, sg);
+                double alp = __shfl_down_sync(kFull, al, sg), bep = __shfl_down_sync(kFull, be, sg),
+                       gap = __shfl_down_sync(kFull, ga, sg);
                 if (k - sg < 0) {
-                    alm = 0.f;
-                    bem = 1.f;
-                    gam = 0.f;
+                    alm = 0.;
+                    bem = 1.;
+                    gam = 0.;
                 }
                 if (k + sg > 31) {
-                    alp = 0.f;
-                    bep = 1.f;
-                    gap = 0.f;
+                    alp = 0.;
+                    bep = 1.;
+                    gap = 0.;
                 }
-                const float ma = (k - sg < 0) ? 0.f : al / bem;
-                const float mc = (k + sg > 31) ? 0.f : ga / bep;
-                ka[lv] = ma;
-                kc[lv] = mc;
-                const float nal = -ma * alm, nga = -mc * gap;
+                const double ma = (k - sg < 0) ? 0. : al / bem;
+                const double mc = (k + sg > 31) ? 0. : ga / bep;
+                ka[lv] = (float)ma;
+                kc[lv] = (float)mc;
+                const double nal = -ma * alm, nga = -mc * gap;
                 be = be - ma * gam - mc * alp;
                 al = nal;
                 ga = nga;
             }
-            if (!(be != 0.f) || !isfinite(be)) st = st == KWG_STATUS_OK ? KWG_STATUS_SOLVER : st;
-            ib = 1.f / be;
+            if (!(be != 0.) || !isfinite(be)) st = st == KWG_STATUS_OK ? KWG_STATUS_SOLVER : st;
+            ib = (float)(1. / be);
         }
+        const float blaf = (float)bla, buaf = (float)bua;
         st = __reduce_max_sync(kFull, st);
         const bool run = st == KWG_STATUS_OK;
         float H[M], Lo[M];  // V as float-float pairs, starting at the payoff
@@ -258,7 +285,7 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
             // separators: right-hand side, cyclic reduction, back to the interior
             float ylp = __shfl_up_sync(kFull, y[M - 1], 1);
             if (k == 0) ylp = 0.f;
-            float rho = y[0] - bla * ylp - bua * y[1];
+            float rho = y[0] - blaf * ylp - buaf * y[1];
 #pragma unroll
             for (int lv = 0; lv < 5; ++lv) {
                 const int sg = 1 << lv;
