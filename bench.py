@@ -53,9 +53,10 @@ def node_steps(n, x_dim=None, t_dim=None):
 
 
 # Algorithmic traffic of the FP64 streaming solve per node and step: V and the sweep
-# value read and written (4 x 8 B), four factor coefficients read (4 x 8 B).
-FP64_BYTES_PER_NODE_STEP = 64
-FP64_FLOPS_PER_NODE_STEP = 8  # 3 FMA + 1 MUL
+# value read and written (32 B) plus, outside the uniform grid's frozen middle region,
+# three factor coefficients and the payoff (32 B; inside it only the payoff, 8 B).
+# The kernel counts these bytes itself (kwg_profile_read).
+FP64_FLOPS_PER_NODE_STEP = 6  # 3 FMA per node-step at theta = 1/2
 
 
 def dist_env():
@@ -140,6 +141,19 @@ def cpu_oracle_rate(opts_all, budget_s=12.0):
         if dt >= budget_s / 4 or n >= len(opts_all):
             return n / dt, threads, n, dt
         n = min(len(opts_all), int(n * max(2.0, budget_s / 4 / max(dt, 1e-3))))
+
+
+def measured_traffic(ns):
+    """DRAM bytes per solve launch from the committed ncu summary (dram__bytes_read +
+    dram__bytes_write of one captured launch, per node-step), scaled to ns node-steps."""
+    path = os.path.join(ROOT, "profiles", "fd1d_solve_fp64_config2.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic per full launch (bytes):"):
+                return float(line.split(":")[1]) / node_steps(32768, 1024, 1024) * ns
+    except (OSError, ValueError):
+        pass
+    return None
 
 
 def fp64_peak_tflops(dev):
@@ -281,7 +295,7 @@ def run_ours(args):
     e1.record(stream)
     barrier()
     clk = clocks.stop()
-    solve_ms, solve_n = ctx.profile_read()
+    solve_ms, solve_n, solve_bytes = ctx.profile_read(with_bytes=True)
     ctx.set_profiling(False)
     ms = max_over_ranks(e0.elapsed_time(e1))
     value = ws * N_OPTIONS * args.steps / (ms / 1e3)
@@ -341,15 +355,10 @@ def run_ours(args):
     hbm, peak_src = peaks()
     per_launch_s = solve_ms / 1e3 / max(solve_n, 1)
     ns = node_steps(N_OPTIONS)
-    achieved = FP64_BYTES_PER_NODE_STEP * ns / per_launch_s / 1e9
+    bytes_per_launch = solve_bytes / max(solve_n, 1)
+    achieved = bytes_per_launch / per_launch_s / 1e9
     fp64_tflops = FP64_FLOPS_PER_NODE_STEP * ns / per_launch_s / 1e12
-    traffic = None
-    prof_file = os.path.join(ROOT, "profiles", "fd1d_solve_fp64_traffic.json")
-    if os.path.exists(prof_file):
-        try:
-            traffic = json.load(open(prof_file)).get("bytes_per_launch_full_size")
-        except ValueError:
-            traffic = None
+    traffic = measured_traffic(ns)
 
     err, nerr = fp64_error_sample(opts, gpu_prices)
     if err > 1e-10:
@@ -377,7 +386,8 @@ def run_ours(args):
         "clocks": clk,
         "roofline": {"bound": "hbm", "kernel": "fd1d_solve_fp64", "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_src, "traffic": traffic,
-                     "algorithmic_bytes_per_node_step": FP64_BYTES_PER_NODE_STEP,
+                     "algorithmic_bytes_per_launch": bytes_per_launch,
+                     "algorithmic_bytes_per_node_step": bytes_per_launch / ns,
                      "node_steps_per_launch": ns, "launch_ms": per_launch_s * 1e3,
                      "fp64_tflops": fp64_tflops, "fp64_peak_tflops": fp64_peak,
                      "fp64_frac": fp64_tflops / fp64_peak if fp64_peak else None,

@@ -130,11 +130,13 @@ int kwg_fd1d_price_device_static(const kwg_option* d_opts, size_t n, const kwg_f
 int kwg_last_launch_count(const kwg_ctx* ctx);
 
 /* Kernel timing for roofline accounting.  With profiling on, every pricing call
- * records CUDA events around its solve kernel on the stream it launches on;
- * kwg_profile_read waits for them, returns the summed solve-kernel time (ms) and the
- * number of launches since the last read, and starts a new accumulation. */
+ * records CUDA events around its solve kernel on the stream it launches on, and the
+ * FP64 solve counts the bytes it reads and writes.  kwg_profile_read waits for
+ * them, returns the summed solve-kernel time (ms), the number of launches and the
+ * summed bytes since the last read (any output may be NULL), and starts a new
+ * accumulation. */
 int kwg_set_profiling(kwg_ctx* ctx, int enable);
-int kwg_profile_read(kwg_ctx* ctx, double* solve_ms, int* solve_launches);
+int kwg_profile_read(kwg_ctx* ctx, double* solve_ms, int* solve_launches, double* solve_bytes);
 
 #ifdef __cplusplus
 }

@@ -371,7 +371,7 @@ int launch_m(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fd1d_solve_fp32<M>, 32, smem);
     if (per_sm < 1) per_sm = 1;
     const int blocks = b.m < sms * per_sm ? b.m : sms * per_sm;
-    cudaMemsetAsync(counters, 0, 2 * sizeof(int), stream);
+    cudaMemsetAsync(counters, 0, 4 * sizeof(int), stream);
     if (ev) cudaEventRecord(ev->start, stream);
     fd1d_solve_fp32<M><<<blocks, 32, smem, stream>>>(b, sh, vout, pde_status, counters);
     if (ev) cudaEventRecord(ev->stop, stream);

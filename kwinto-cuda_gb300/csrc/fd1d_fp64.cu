@@ -9,26 +9,36 @@
 // B = 1 - theta dt A and E = 1 + (1-theta) dt A built row by row from the same
 // operator A.  Because B and E come from one A,
 //     theta E + (1 - theta) B = 1    =>    B^-1 E = (theta B)^-1 - c,  c = (1-theta)/theta,
-// so each step is  y = (theta B)^-1 V,  V' = max(y - c V, payoff).  A, dt and the
-// grid do not change between steps, so theta B is factorised once per PDE:
-//     LU (eliminate upward):   d_0 = T_0;  l_j = Tl_j/d_{j-1},  d_j = Tm_j - l_j Tu_{j-1}
-//     UL (eliminate downward): e_{N-1} = Tm;  m_j = Tu_j/e_{j+1}, e_j = Tm_j - m_j Tl_{j+1}
+// so each step is  y = T^-1 V  (T = theta B),  V' = max(y - cV, p).  A, dt and the
+// grid do not change between steps, so T is factorised once per PDE, both ways:
+//     LU (eliminate upward):   d_0 = Tm_0,  d_j = Tm_j - Tl_j Tu_{j-1} / d_{j-1}
+//     UL (eliminate downward): e_{N-1} = Tm_{N-1},  e_j = Tm_j - Tu_j Tl_{j+1} / e_{j+1}
 // and the steps alternate between them, so the back substitution of one step and
-// the forward elimination of the next run in ONE sweep over the nodes:
-//     UP sweep   (j = 0..N-1):  y_j = k_j - n_j y_{j-1}      (back-substitute UL)
-//                               V_j = max(y_j - c V_j, p_j)
-//                               f_j = V_j - l_j f_{j-1},  g_j = f_j / d_j   (eliminate LU)
-//     DOWN sweep (j = N-1..0):  y_j = g_j - u_j y_{j+1}      (back-substitute LU)
-//                               V_j = max(y_j - c V_j, p_j)
-//                               h_j = V_j - m_j h_{j+1},  k_j = h_j / e_j   (eliminate UL)
-// Four FP64 operations per node and step (the reference does ~40 plus 5 divisions),
-// one read and one write of (V, k|g) per node and step, and four coefficients read.
+// the forward elimination of the next run in ONE sweep over the nodes.  The
+// elimination results are kept unscaled and the back substitution carries
+// yh = y * pivot, which folds the pivot scaling into the update:
+//   UP   (j = 0..N-1):  yh = h - nh*yh_prev    nh = Tl_j/e_{j-1}   (back-substitute UL)
+//                       V  = max(yh/e - cV, p)
+//                       f  = V - l*f_prev     l  = Tl_j/d_{j-1}   (eliminate LU)
+//   DOWN (j = N-1..0):  yh = f - uh*yh_prev    uh = Tu_j/d_{j+1}   (back-substitute LU)
+//                       V  = max(yh/d - cV, p)
+//                       h  = V - m*h_prev     m  = Tu_j/e_{j+1}   (eliminate UL)
+// Three FP64 operations per node and step when theta = 1/2 (c = 1), four otherwise;
+// the reference does ~40 plus 5 divisions.  max() runs on the integer pipe.
 //
-// Layout (option-interleaved, one tile = 32 PDEs = one warp, lane = PDE): one record
-// of 10 fields x 32 lanes (2.5 KB) per node,
-//     [0] p  [1] n  [2] l  [3] 1/d  |  [4] V  [5] k|g  |  [6] p  [7] u  [8] m  [9] 1/e
-// so an UP sweep reads fields 0..5 and a DOWN sweep fields 4..9: one contiguous
-// 1.5 KB bulk copy per node and warp, and a lane's field is a 256-byte line's slot.
+// Uniform grids (density = +inf).  Rows come from the exact spacing h, so interior
+// rows are identical; the pivot recurrences d_j, e_j then converge and are frozen at
+// their limit (a change of an ulp or two).  Nodes whose six coefficients are all
+// frozen form a middle region where a sweep streams only (p, V, state).
+//
+// Layout (option-interleaved, one tile = 32 PDEs = one warp, lane = PDE), arrays per
+// tile and node so that a run of consecutive nodes is contiguous for each sweep:
+//     CU [node][3][32]  UP coefficients   (nh, l, 1/e)
+//     CD [node][3][32]  DOWN coefficients (uh, m, 1/d)
+//     P  [node][32]     payoff
+//     S  [node][32][2]  state (V, h|f), one 16-byte load/store per lane
+// A sweep streams them in stages of kGroup consecutive nodes (one mbarrier, two or
+// three bulk copies per stage); in the middle region the coefficients are not read.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -40,23 +50,68 @@ namespace kwg {
 
 namespace {
 
-constexpr int kFields = 10;
-constexpr int F_UP_P = 0, F_UP_N = 1, F_UP_L = 2, F_UP_ID = 3;
-constexpr int F_V = 4, F_W = 5;
-constexpr int F_DN_P = 6, F_DN_U = 7, F_DN_M = 8, F_DN_IE = 9;
-constexpr int kSweepFields = 6;                         // fields one sweep reads
-constexpr uint32_t kStageBytes = kSweepFields * kTile * 8;  // 1536 B
-
-__device__ __forceinline__ size_t rec_idx(int j, int f) { return ((size_t)j * kFields + f) * kTile; }
+constexpr int kCoef = 3;                                   // coefficients per node and sweep
+constexpr int kConsts = 6;                                 // nh l 1/e uh m 1/d in the middle
+constexpr int kGroup = 4;                                  // nodes per stage
+constexpr uint32_t kNodeCoefBytes = kCoef * kTile * 8;    // 768 B
+constexpr uint32_t kNodePBytes = kTile * 8;               // 256 B
+constexpr uint32_t kNodeSBytes = 2 * kTile * 8;           // 512 B
 
 __device__ __forceinline__ bool finite_nonzero(double v) { return v != 0. && isfinite(v); }
+
+// Work buffer: CU, CD, P, S (each [tile][node]...), then per-PDE middle constants and
+// the middle range.
+struct Work {
+    double* cu;
+    double* cd;
+    double* p;
+    double* s;
+    double* cst;  // [m_pad][6]
+    int2* range;  // [m_pad]: first and last node of the middle region (empty: x > y)
+};
+
+__device__ __forceinline__ Work work_of(double* base, int m_pad, int n)
+{
+    const size_t nodes = (size_t)m_pad * n;
+    Work w;
+    w.cu = base;
+    w.cd = w.cu + nodes * kCoef;
+    w.p = w.cd + nodes * kCoef;
+    w.s = w.p + nodes;
+    w.cst = w.s + nodes * 2;
+    w.range = reinterpret_cast<int2*>(w.cst + (size_t)m_pad * kConsts);
+    return w;
+}
+
+// Per-tile views (lane 0's element of node 0).
+struct TileView {
+    double* cu;
+    double* cd;
+    double* p;
+    double* s;
+};
+
+__device__ __forceinline__ TileView tile_view(const Work& w, int tile, int n)
+{
+    TileView v;
+    const size_t base = (size_t)tile * n * kTile;
+    v.cu = w.cu + base * kCoef;
+    v.cd = w.cd + base * kCoef;
+    v.p = w.p + base;
+    v.s = w.s + base * 2;
+    return v;
+}
+
+// The pivot recurrences are frozen once a step changes them by at most this
+// relative amount (uniform grids only, where the interior rows are identical).
+constexpr double kFreeze = 0x1p-50;
 
 }  // namespace
 
 // One thread per PDE slot.  Builds the grid, payoff and both factorisations of
-// theta*B, writes the node records, V = payoff, and runs the first (DOWN)
-// elimination on V so that the solve kernel starts with an UP sweep.
-__global__ void __launch_bounds__(128) fd1d_setup_fp64(const PdeBatch b, Fd1dShape sh, double* __restrict__ rec,
+// theta*B, writes CU, CD, P, S (V = payoff), the middle-region constants, and runs
+// the first (DOWN) elimination on V so that the solve starts with an UP sweep.
+__global__ void __launch_bounds__(128) fd1d_setup_fp64(const PdeBatch b, Fd1dShape sh, double* __restrict__ base,
                                                        int32_t* __restrict__ pde_status)
 {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
@@ -64,7 +119,12 @@ __global__ void __launch_bounds__(128) fd1d_setup_fp64(const PdeBatch b, Fd1dSha
     const int src = slot < b.m ? slot : b.m - 1;  // padding lanes replicate the last PDE
     const int tile = slot / kTile, lane = slot % kTile;
     const int N = sh.x_dim;
-    double* R = rec + (size_t)tile * N * kFields * kTile + lane;
+    const Work wk = work_of(base, b.m_pad, N);
+    const TileView tv = tile_view(wk, tile, N);
+    auto CU = [&](int j, int f) -> double& { return tv.cu[((size_t)j * kCoef + f) * kTile + lane]; };
+    auto CD = [&](int j, int f) -> double& { return tv.cd[((size_t)j * kCoef + f) * kTile + lane]; };
+    auto P = [&](int j) -> double& { return tv.p[(size_t)j * kTile + lane]; };
+    auto S = [&](int j, int f) -> double& { return tv.s[((size_t)j * kTile + lane) * 2 + f]; };
 
     const double t = b.t[src], z = b.z[src];
     const int8_t w = b.w[src];
@@ -78,110 +138,252 @@ __global__ void __launch_bounds__(128) fd1d_setup_fp64(const PdeBatch b, Fd1dSha
     const Coef a = pde_coef(b.r[src], b.q[src], z);
     const double dt = time_step(t, sh.t_dim);
     const double theta = sh.theta;
+    // uniform grids: rows from the exact spacing, so interior rows are identical
+    const double hx = sh.uniform ? dvd(sub(g.xMax, g.xMin), (double)(N - 1)) : 0.;
 
-    // Upward sweep: rows, payoff, LU of theta*B.  Tl, Tu, Tm are parked in the
-    // n, m, 1/e slots for the downward sweep.
+    // Upward pass: rows, payoff, LU pivots d_j.  Tl is parked in CU.nh; d_j, Tu, Tm
+    // in CD (uh, m, 1/d) for the downward pass.
     double xm = 0., x0 = g.x(0), xp = g.x(1);
     double d_prev = 1., tu_prev = 0.;
+    bool lu_frozen = false;
+    int lu_freeze = N;  // first j whose d_j was frozen
     for (int j = 0; j < N; ++j) {
         if (j > 0) {
             xm = x0;
             x0 = xp;
             xp = (j + 1 < N) ? g.x(j + 1) : 0.;
         }
-        const Row r = implicit_row(j, N, xm, x0, xp, theta, dt, a.a0, a.ax, a.axx);
+        const Row r = sh.uniform ? implicit_row(j, N, -hx, 0., hx, theta, dt, a.a0, a.ax, a.axx)
+                                 : implicit_row(j, N, xm, x0, xp, theta, dt, a.a0, a.ax, a.axx);
         const double tl = mul(theta, r.bl), tm = mul(theta, r.b), tu = mul(theta, r.bu);
         const double p = payoff(w, x0);
-        double l = 0., d = tm;
+        double d = tm;
         if (j > 0) {
-            l = dvd(tl, d_prev);
-            d = sub(tm, mul(l, tu_prev));
+            if (lu_frozen && j < N - 1) {
+                d = d_prev;
+            } else {
+                d = sub(tm, mul(dvd(tl, d_prev), tu_prev));
+                if (sh.uniform && j >= 3 && j < N - 1 && fabs(d - d_prev) <= kFreeze * fabs(d)) {
+                    lu_frozen = true;
+                    lu_freeze = j;
+                    d = d_prev;
+                }
+            }
         }
         if (!finite_nonzero(d) && st == KWG_STATUS_OK) st = KWG_STATUS_SOLVER;
-        const double id = dvd(1., d);
-        R[rec_idx(j, F_UP_P)] = p;
-        R[rec_idx(j, F_UP_N)] = tl;  // parked
-        R[rec_idx(j, F_UP_L)] = l;
-        R[rec_idx(j, F_UP_ID)] = id;
-        R[rec_idx(j, F_V)] = p;
-        R[rec_idx(j, F_DN_P)] = p;
-        R[rec_idx(j, F_DN_U)] = mul(tu, id);
-        R[rec_idx(j, F_DN_M)] = tu;   // parked
-        R[rec_idx(j, F_DN_IE)] = tm;  // parked
+        CU(j, 0) = tl;  // parked
+        CU(j, 1) = j > 0 ? dvd(tl, d_prev) : 0.;
+        P(j) = p;
+        S(j, 0) = p;
+        CD(j, 0) = d;   // parked
+        CD(j, 1) = tu;  // parked
+        CD(j, 2) = tm;  // parked
         d_prev = d;
         tu_prev = tu;
     }
-    // Downward sweep: UL of theta*B, then the first elimination (DOWN) of V = payoff.
-    double e_next = 1., tl_next = 0., h_next = 0.;
+    // Downward pass: UL pivots e_j; final coefficients; first elimination of V = p.
+    double e_next = 1., tl_next = 0., h_next = 0., d_next = 1.;
+    bool ul_frozen = false;
+    int ul_freeze = -1;  // first j (from the top) whose e_j was frozen
     for (int j = N - 1; j >= 0; --j) {
-        const double tl = R[rec_idx(j, F_UP_N)];
-        const double tu = R[rec_idx(j, F_DN_M)];
-        const double tm = R[rec_idx(j, F_DN_IE)];
-        double m = 0., e = tm;
+        const double tl = CU(j, 0), d = CD(j, 0), tu = CD(j, 1), tm = CD(j, 2);
+        double e = tm, m = 0.;
         if (j < N - 1) {
             m = dvd(tu, e_next);
-            e = sub(tm, mul(m, tl_next));
+            if (ul_frozen && j > 0) {
+                e = e_next;
+            } else {
+                e = sub(tm, mul(m, tl_next));
+                if (sh.uniform && j <= N - 4 && j > 0 && fabs(e - e_next) <= kFreeze * fabs(e)) {
+                    ul_frozen = true;
+                    ul_freeze = j;
+                    e = e_next;
+                }
+            }
         }
         if (!finite_nonzero(e) && st == KWG_STATUS_OK) st = KWG_STATUS_SOLVER;
-        const double ie = dvd(1., e);
-        R[rec_idx(j, F_UP_N)] = dvd(tl, e);
-        R[rec_idx(j, F_DN_M)] = m;
-        R[rec_idx(j, F_DN_IE)] = ie;
-        const double p = R[rec_idx(j, F_V)];
-        const double h = fma(-m, h_next, p);
-        R[rec_idx(j, F_W)] = mul(h, ie);
+        // row j+1's nh = Tl_{j+1} / e_j, written now that e_j is known
+        if (j < N - 1) CU(j + 1, 0) = dvd(tl_next, e);
+        CU(j, 2) = dvd(1., e);
+        CD(j, 0) = j < N - 1 ? dvd(tu, d_next) : 0.;
+        CD(j, 1) = m;
+        CD(j, 2) = dvd(1., d);
+        const double h = fma(-m, h_next, P(j));
+        S(j, 1) = h;
         e_next = e;
         tl_next = tl;
         h_next = h;
+        d_next = d;
     }
+    CU(0, 0) = 0.;  // Tl_0 = 0
+
+    // Middle region: nodes whose coefficients (built from d and e at j-1..j+1 and
+    // interior rows j-1..j+1) are all frozen.
+    int lo = N, hi = -1;
+    if (sh.uniform && lu_frozen && ul_frozen) {
+        lo = max(lu_freeze + 1, 2);
+        hi = min(ul_freeze - 1, N - 3);
+    }
+    if (lo <= hi) {
+        const int mid = (lo + hi) / 2;
+        double* c = wk.cst + (size_t)slot * kConsts;
+        c[0] = CU(mid, 0);
+        c[1] = CU(mid, 1);
+        c[2] = CU(mid, 2);
+        c[3] = CD(mid, 0);
+        c[4] = CD(mid, 1);
+        c[5] = CD(mid, 2);
+    }
+    wk.range[slot] = make_int2(lo, hi);
     if (slot < b.m) pde_status[slot] = st;
 }
 
 namespace {
 
-// Ring of node stages in shared memory, filled by one bulk copy each.  Visits are
-// numbered globally per warp (q); visit q uses stage q % kRing with mbarrier
-// parity (q / kRing) & 1.
-constexpr int kRing = 16;
+// Ring of stages in shared memory; a stage holds kGroup consecutive nodes of one
+// sweep: coefficients [kGroup][3][32], payoff [kGroup][32], state [kGroup][32][2].
+// Stage visits are numbered per warp (q); visit q uses stage q % kRing with
+// mbarrier parity (q / kRing) & 1.
+constexpr int kRing = 4;
+constexpr uint32_t kStageCoef = kGroup * kNodeCoefBytes;  // 3 KB
+constexpr uint32_t kStageP = kGroup * kNodePBytes;        // 1 KB
+constexpr uint32_t kStageS = kGroup * kNodeSBytes;        // 2 KB
+constexpr uint32_t kStageBytes = kStageCoef + kStageP + kStageS;
 constexpr size_t kSolveSmem = kRing * kStageBytes + kRing * sizeof(uint64_t);
 
 struct Ring {
-    double* stage;  // kRing * 6 * 32 doubles
-    uint64_t* bar;  // kRing mbarriers
+    unsigned char* stage;  // kRing * kStageBytes
+    uint64_t* bar;         // kRing mbarriers
 };
 
-__device__ __forceinline__ void issue(const Ring& r, uint64_t q, const double* src)
+// Nodes of stage number g of a sweep: [first, first + count), ascending in memory.
+template <bool kUp>
+__device__ __forceinline__ void stage_nodes(int g, int N, int& first, int& count)
 {
-    const int s = (int)(q % kRing);
-    mbar_arrive_expect_tx(&r.bar[s], kStageBytes);
-    bulk_g2s(r.stage + (size_t)s * kSweepFields * kTile, src, kStageBytes, &r.bar[s]);
+    if (kUp) {
+        first = g * kGroup;
+        count = min(kGroup, N - first);
+    } else {
+        const int top = N - 1 - g * kGroup;
+        first = max(top - kGroup + 1, 0);
+        count = top - first + 1;
+    }
 }
 
-// Bounded wait for visits [from, to) after a timeout: lets copies in flight land in
-// shared memory before the block exits.
-__device__ void drain(const Ring& r, uint64_t from, uint64_t to)
+// A stage skips the coefficients when all its nodes lie in the middle region.
+__device__ __forceinline__ bool stage_compact(int first, int count, int lo, int hi)
 {
-    for (uint64_t q = from; q < to; ++q) mbar_wait(&r.bar[q % kRing], (uint32_t)((q / kRing) & 1));
+    return first >= lo && first + count - 1 <= hi;
+}
+
+// Issues stage visit q covering sweep stage g of this tile.
+template <bool kUp>
+__device__ __forceinline__ void issue(const Ring& r, uint32_t q, const TileView& tv, int g, int N, int lo, int hi)
+{
+    int first, count;
+    stage_nodes<kUp>(g, N, first, count);
+    const bool compact = stage_compact(first, count, lo, hi);
+    const int s = (int)(q % kRing);
+    unsigned char* st = r.stage + (size_t)s * kStageBytes;
+    const uint32_t cb = compact ? 0u : count * kNodeCoefBytes;
+    const uint32_t pb = count * kNodePBytes, sb = count * kNodeSBytes;
+    mbar_arrive_expect_tx(&r.bar[s], cb + pb + sb);
+    if (!compact) bulk_g2s(st, (kUp ? tv.cu : tv.cd) + (size_t)first * kCoef * kTile, cb, &r.bar[s]);
+    bulk_g2s(st + kStageCoef, tv.p + (size_t)first * kTile, pb, &r.bar[s]);
+    bulk_g2s(st + kStageCoef + kStageP, tv.s + (size_t)first * kTile * 2, sb, &r.bar[s]);
+}
+
+// Bounded wait for stage visits [from, to) after a timeout: lets copies in flight
+// land in shared memory before the block exits.
+__device__ void drain(const Ring& r, uint32_t from, uint32_t to)
+{
+    for (uint32_t q = from; q < to; ++q) mbar_wait(&r.bar[q % kRing], (q / kRing) & 1u);
+}
+
+// One sweep over this warp's tile.  Returns false on a wait timeout (already drained).
+template <bool kUp, bool kHalf>
+__device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileView& tv, int lane, int N, int lo,
+                                      int hi, const double* cst, double c, bool amer, int* err)
+{
+    const int ng = (N + kGroup - 1) / kGroup;
+    const int pre = ng < kRing ? ng : kRing;
+    // the previous sweep's stores must be visible to the bulk-copy engine
+    fence_proxy_async_global();
+    __syncwarp();
+    if (lane == 0)
+        for (int g = 0; g < pre; ++g) issue<kUp>(ring, q + g, tv, g, N, lo, hi);
+    // middle-region constants: UP uses (nh, l, 1/e), DOWN (uh, m, 1/d)
+    const double ca = kUp ? cst[0] : cst[3], cb = kUp ? cst[1] : cst[4], cs = kUp ? cst[2] : cst[5];
+    double2* sout = reinterpret_cast<double2*>(tv.s) + lane;
+    double yh = 0., f = 0.;
+    for (int g = 0; g < ng; ++g) {
+        const uint32_t v = q + g;
+        const int s = (int)(v % kRing);
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(&ring.bar[s], (v / kRing) & 1u));
+        if (!ok) {
+            if (lane == 0) {
+                atomicExch(err, 1);
+                drain(ring, v, q + min(g + kRing, ng));
+            }
+            __syncwarp();
+            return false;
+        }
+        int first, count;
+        stage_nodes<kUp>(g, N, first, count);
+        const bool compact = stage_compact(first, count, lo, hi);
+        const unsigned char* st = ring.stage + (size_t)s * kStageBytes;
+        const double* sc_ = reinterpret_cast<const double*>(st) + lane;
+        const double* sp_ = reinterpret_cast<const double*>(st + kStageCoef) + lane;
+        const double2* ss_ = reinterpret_cast<const double2*>(st + kStageCoef + kStageP) + lane;
+        double ra[kGroup], rb[kGroup], rs[kGroup], rp[kGroup], rv[kGroup], rw[kGroup];
+#pragma unroll
+        for (int k = 0; k < kGroup; ++k) {
+            const int idx = kUp ? k : count - 1 - k;  // processing order within the stage
+            if (k < count) {
+                rp[k] = sp_[idx * kTile];
+                const double2 sv = ss_[idx * kTile];
+                rv[k] = sv.x;
+                rw[k] = sv.y;
+                ra[k] = compact ? ca : sc_[(idx * kCoef + 0) * kTile];
+                rb[k] = compact ? cb : sc_[(idx * kCoef + 1) * kTile];
+                rs[k] = compact ? cs : sc_[(idx * kCoef + 2) * kTile];
+            }
+        }
+        __syncwarp();  // stage s fully read before it is refilled
+        if (lane == 0 && g + kRing < ng) issue<kUp>(ring, v + kRing, tv, g + kRing, N, lo, hi);
+#pragma unroll
+        for (int k = 0; k < kGroup; ++k) {
+            if (k < count) {
+                const int j = kUp ? first + k : first + count - 1 - k;
+                yh = fma(-ra[k], yh, rw[k]);
+                double vn = kHalf ? fma(rs[k], yh, -rv[k]) : fma(rs[k], yh, -c * rv[k]);
+                if (amer && j < N - 1) vn = max_floor(vn, rp[k]);
+                f = fma(-rb[k], f, vn);
+                sout[(size_t)j * kTile] = make_double2(vn, f);
+            }
+        }
+    }
+    return true;
 }
 
 }  // namespace
 
 // Persistent: each warp takes tiles from tile_counter[0] (zeroed by the host before
 // the launch) and runs all tDim-1 steps of its 32 PDEs.  One warp per block so the
-// scheduler spreads warps evenly over the SMs.  The node records stream through a
-// 16-deep shared-memory ring filled by the TMA engine; V and k|g are written back
-// with ordinary stores.  If a ring wait expires, tile_counter[1] is set, the warp
-// drains its copies in flight and leaves; the interpolation kernel then marks every
-// option with KWG_STATUS_DEVICE_TIMEOUT.
-//
-//   UP sweep   (j = 0..N-1):  y = k - n y_prev;  V = max(y - cV, p);  f = V - l f_prev;  g = f/d
-//   DOWN sweep (j = N-1..0):  y = g - u y_prev;  V = max(y - cV, p);  h = V - m h_prev;  k = h/e
-__global__ void __launch_bounds__(32) fd1d_solve_fp64(const PdeBatch b, Fd1dShape sh, double* __restrict__ rec,
+// scheduler spreads warps evenly over the SMs.  The sweeps stream through a 4-deep
+// ring of 4-node stages in shared memory filled by the TMA engine; V and h|f are
+// written back with ordinary 16-byte stores.  If a ring wait expires,
+// tile_counter[1] is set, the warp drains its copies in flight and leaves; the
+// interpolation kernel then marks every option with KWG_STATUS_DEVICE_TIMEOUT.
+// tile_counter[2..3] accumulates (64-bit) the bytes the launch reads and writes.
+// kHalf: theta = 1/2 (c = 1).
+template <bool kHalf>
+__global__ void __launch_bounds__(32) fd1d_solve_fp64(const PdeBatch b, Fd1dShape sh, double* __restrict__ base,
                                                       int* __restrict__ tile_counter)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     Ring ring;
-    ring.stage = reinterpret_cast<double*>(smem);
+    ring.stage = smem;
     ring.bar = reinterpret_cast<uint64_t*>(smem + kRing * kStageBytes);
     const int lane = threadIdx.x & 31;
     if (lane == 0) {
@@ -191,10 +393,10 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64(const PdeBatch b, Fd1dShap
     __syncwarp();
 
     const int N = sh.x_dim;
+    const int ng = (N + kGroup - 1) / kGroup;
     const int ntiles = b.m_pad / kTile;
-    const double c = sh.c;
-    const int pre = N < kRing ? N : kRing;
-    uint64_t q = 0;  // visits consumed so far
+    const Work wk = work_of(base, b.m_pad, N);
+    uint32_t q = 0;  // stage visits consumed so far
     for (;;) {
         int tile = 0;
         if (lane == 0) tile = atomicAdd(&tile_counter[0], 1);
@@ -203,64 +405,37 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64(const PdeBatch b, Fd1dShap
         const int slot = tile * kTile + lane;
         const int src = slot < b.m ? slot : b.m - 1;
         const bool amer = b.e[src] != 0;
-        double* R0 = rec + (size_t)tile * N * kFields * kTile;  // tile base (lane 0)
-        double* R = R0 + lane;
-        for (int pass = 1; pass < sh.t_dim; ++pass) {
-            const bool up = pass & 1;
-            const int f0 = up ? F_UP_P : F_V;  // first field this sweep reads
-            // the previous sweep's stores must be visible to the bulk-copy engine
-            fence_proxy_async_global();
-            __syncwarp();
-            if (lane == 0)
-                for (int d = 0; d < pre; ++d) {
-                    const int j = up ? d : N - 1 - d;
-                    issue(ring, q + d, R0 + rec_idx(j, f0));
-                }
-            double y = 0., f = 0.;
-            for (int i = 0; i < N; ++i) {
-                const uint64_t v = q + i;
-                const int s = (int)(v % kRing);
-                const bool ok = __all_sync(0xffffffffu, mbar_wait(&ring.bar[s], (uint32_t)((v / kRing) & 1)));
-                if (!ok) {
-                    if (lane == 0) {
-                        atomicExch(&tile_counter[1], 1);
-                        const int issued = (i + kRing < N) ? i + kRing : N;
-                        drain(ring, v, q + issued);
-                    }
-                    __syncwarp();
-                    return;
-                }
-                const double* st = ring.stage + (size_t)s * kSweepFields * kTile + lane;
-                double p, a, bb, sc, vo, w;
-                if (up) {
-                    p = st[0 * kTile];
-                    a = st[1 * kTile];
-                    bb = st[2 * kTile];
-                    sc = st[3 * kTile];
-                    vo = st[4 * kTile];
-                    w = st[5 * kTile];
-                } else {
-                    vo = st[0 * kTile];
-                    w = st[1 * kTile];
-                    p = st[2 * kTile];
-                    a = st[3 * kTile];
-                    bb = st[4 * kTile];
-                    sc = st[5 * kTile];
-                }
-                __syncwarp();  // stage s fully read before it is refilled
-                if (lane == 0 && i + kRing < N) {
-                    const int jn = up ? i + kRing : N - 1 - i - kRing;
-                    issue(ring, v + kRing, R0 + rec_idx(jn, f0));
-                }
-                const int j = up ? i : N - 1 - i;
-                y = fma(-a, y, w);
-                double vn = fma(-c, vo, y);
-                if (amer && j < N - 1) vn = max_floor(vn, p);
-                f = fma(-bb, f, vn);
-                R[rec_idx(j, F_V)] = vn;
-                R[rec_idx(j, F_W)] = f * sc;
+        const TileView tv = tile_view(wk, tile, N);
+        // the tile's middle region is where every lane's coefficients are frozen
+        const int2 rg = wk.range[slot];
+        const int lo = __reduce_max_sync(0xffffffffu, rg.x);
+        const int hi = __reduce_min_sync(0xffffffffu, rg.y);
+        double cst[kConsts] = {0., 0., 0., 0., 0., 0.};
+        if (lo <= hi)
+            for (int k = 0; k < kConsts; ++k) cst[k] = wk.cst[(size_t)slot * kConsts + k];
+        if (lane == 0) {
+            // bytes this tile moves per sweep: the stages' bulk reads + the state stores
+            unsigned long long per_up = 0, per_dn = 0;
+            for (int g = 0; g < ng; ++g) {
+                int first, count;
+                stage_nodes<true>(g, N, first, count);
+                per_up += count * (kNodePBytes + 2 * kNodeSBytes) +
+                          (stage_compact(first, count, lo, hi) ? 0 : count * kNodeCoefBytes);
+                stage_nodes<false>(g, N, first, count);
+                per_dn += count * (kNodePBytes + 2 * kNodeSBytes) +
+                          (stage_compact(first, count, lo, hi) ? 0 : count * kNodeCoefBytes);
             }
-            q += N;
+            const unsigned long long n_up = (unsigned long long)(sh.t_dim / 2);  // passes 1, 3, 5, ...
+            const unsigned long long n_dn = (unsigned long long)((sh.t_dim - 1) / 2);
+            atomicAdd(reinterpret_cast<unsigned long long*>(tile_counter + 2), per_up * n_up + per_dn * n_dn);
+        }
+        for (int pass = 1; pass < sh.t_dim; ++pass) {
+            const bool ok = (pass & 1) ? sweep<true, kHalf>(ring, q, tv, lane, N, lo, hi, cst, sh.c, amer,
+                                                            &tile_counter[1])
+                                       : sweep<false, kHalf>(ring, q, tv, lane, N, lo, hi, cst, sh.c, amer,
+                                                             &tile_counter[1]);
+            if (!ok) return;
+            q += ng;
         }
     }
 }
@@ -268,10 +443,9 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64(const PdeBatch b, Fd1dShap
 // One thread per asset: x* = log(s/k), first node x_i >= x* (binary search on the
 // grid, the same node the reference's linear search finds, src/Math/kwFd1d.cpp:
 // 145-147), linear interpolation (:156), price = k*V (src/Pricer/kwFd1d.cpp:156).
-__global__ void fd1d_interp_fp64(const PdeBatch b, const AssetBatch a, Fd1dShape sh,
-                                 const double* __restrict__ rec, const int32_t* __restrict__ pde_status,
-                                 const int* __restrict__ device_error, double* __restrict__ prices,
-                                 int32_t* __restrict__ status)
+__global__ void fd1d_interp_fp64(const PdeBatch b, const AssetBatch a, Fd1dShape sh, double* __restrict__ base,
+                                 const int32_t* __restrict__ pde_status, const int* __restrict__ device_error,
+                                 double* __restrict__ prices, int32_t* __restrict__ status)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
@@ -297,10 +471,11 @@ __global__ void fd1d_interp_fp64(const PdeBatch b, const AssetBatch a, Fd1dShape
         if (lo == 0 || lo == N) {
             st = KWG_STATUS_OUT_OF_GRID;
         } else {
-            const int tile = slot / kTile, lane = slot % kTile;
-            const double* R = rec + (size_t)tile * N * kFields * kTile + lane;
+            const TileView tv = tile_view(work_of(base, b.m_pad, N), slot / kTile, N);
+            const int lane = slot % kTile;
             const double xl = g.x(lo - 1), xh = g.x(lo);
-            const double vl = R[rec_idx(lo - 1, F_V)], vh = R[rec_idx(lo, F_V)];
+            const double vl = tv.s[((size_t)(lo - 1) * kTile + lane) * 2];
+            const double vh = tv.s[((size_t)lo * kTile + lane) * 2];
             const double v = dvd(add(mul(sub(xh, xs), vl), mul(sub(xs, xl), vh)), sub(xh, xl));
             price = mul(k, v);
         }
@@ -315,7 +490,7 @@ int fd1d_fp64_solve_blocks(int ntiles, int device)
     if (cached_dev != device) {
         cudaDeviceGetAttribute(&cached_sms, cudaDevAttrMultiProcessorCount, device);
         cached_max = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_max, fd1d_solve_fp64, 32, kSolveSmem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_max, fd1d_solve_fp64<true>, 32, kSolveSmem);
         if (cached_max < 1) cached_max = 1;
         cached_dev = device;
     }
@@ -323,22 +498,33 @@ int fd1d_fp64_solve_blocks(int ntiles, int device)
     return ntiles < cap ? (ntiles > 0 ? ntiles : 1) : cap;
 }
 
-size_t fd1d_fp64_work_bytes(int m_pad, int x_dim) { return (size_t)m_pad * x_dim * kFields * sizeof(double); }
+size_t fd1d_fp64_work_bytes(int m_pad, int x_dim)
+{
+    return (size_t)m_pad * x_dim * (2 * kCoef + 1 + 2) * sizeof(double) + (size_t)m_pad * kConsts * sizeof(double) +
+           (size_t)m_pad * sizeof(int2);
+}
 
-int fd1d_fp64_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* rec, int32_t* pde_status,
+int fd1d_fp64_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* work, int32_t* pde_status,
                      int* counters, double* prices, int32_t* status, int solve_blocks, cudaStream_t stream,
                      const SolveEvents* ev)
 {
     int launches = 0;
-    fd1d_setup_fp64<<<(b.m_pad + 127) / 128, 128, 0, stream>>>(b, sh, rec, pde_status);
+    fd1d_setup_fp64<<<(b.m_pad + 127) / 128, 128, 0, stream>>>(b, sh, work, pde_status);
     ++launches;
-    cudaMemsetAsync(counters, 0, 2 * sizeof(int), stream);
+    cudaMemsetAsync(counters, 0, 4 * sizeof(int), stream);
     if (ev) cudaEventRecord(ev->start, stream);
-    fd1d_solve_fp64<<<solve_blocks, 32, kSolveSmem, stream>>>(b, sh, rec, counters);
-    if (ev) cudaEventRecord(ev->stop, stream);
+    if (sh.c == 1.)
+        fd1d_solve_fp64<true><<<solve_blocks, 32, kSolveSmem, stream>>>(b, sh, work, counters);
+    else
+        fd1d_solve_fp64<false><<<solve_blocks, 32, kSolveSmem, stream>>>(b, sh, work, counters);
+    if (ev) {
+        cudaEventRecord(ev->stop, stream);
+        if (ev->bytes) cudaMemcpyAsync(ev->bytes, counters + 2, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                       stream);
+    }
     ++launches;
     if (a.n > 0) {
-        fd1d_interp_fp64<<<(a.n + 127) / 128, 128, 0, stream>>>(b, a, sh, rec, pde_status, counters + 1, prices,
+        fd1d_interp_fp64<<<(a.n + 127) / 128, 128, 0, stream>>>(b, a, sh, work, pde_status, counters + 1, prices,
                                                                  status);
         ++launches;
     }

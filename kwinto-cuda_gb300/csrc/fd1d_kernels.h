@@ -48,10 +48,12 @@ size_t fd1d_fp64_work_bytes(int m_pad, int x_dim);
 // Optional CUDA events recorded immediately before and after the solve kernel.
 struct SolveEvents {
     cudaEvent_t start = nullptr, stop = nullptr;
+    unsigned long long* bytes = nullptr;  // pinned host slot for the launch's byte count
 };
 
 // Launches setup, solve and interpolation on `stream`; returns the launch count.
-// counters: 2 ints, [0] tile queue, [1] device-timeout flag (zeroed here).
+// counters: 4 ints, [0] tile queue, [1] device-timeout flag, [2..3] a 64-bit count
+// of the bytes the solve reads and writes (all zeroed here).
 int fd1d_fp64_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* rec, int32_t* pde_status,
                      int* counters, double* prices, int32_t* status, int solve_blocks, cudaStream_t stream,
                      const SolveEvents* ev);

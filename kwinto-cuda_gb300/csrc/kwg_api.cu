@@ -34,7 +34,7 @@ struct kwg_ctx {
     size_t work_bytes = 0;
     void* d_io = nullptr;  // packed inputs / outputs
     size_t io_bytes = 0;
-    int* d_counter = nullptr;  // [0] tile queue, [1] device-timeout flag
+    int* d_counter = nullptr;  // [0] tile queue, [1] device-timeout flag, [2..3] 64-bit byte count
     // pinned host staging
     void* h_io = nullptr;
     size_t h_io_bytes = 0;
@@ -48,9 +48,12 @@ struct kwg_ctx {
         if (!profiling) return nullptr;
         if (events_used == events.size()) {
             kwg::SolveEvents e;
-            if (cudaEventCreate(&e.start) != cudaSuccess || cudaEventCreate(&e.stop) != cudaSuccess) return nullptr;
+            if (cudaEventCreate(&e.start) != cudaSuccess || cudaEventCreate(&e.stop) != cudaSuccess ||
+                cudaMallocHost(&e.bytes, sizeof(unsigned long long)) != cudaSuccess)
+                return nullptr;
             events.push_back(e);
         }
+        *events[events_used].bytes = 0;
         return &events[events_used++];
     }
 };
@@ -255,7 +258,7 @@ kwg_ctx* kwg_create(int device)
     ctx->device = device;
     cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMalloc(&ctx->d_counter, 2 * sizeof(int)) != cudaSuccess) {
+        cudaMalloc(&ctx->d_counter, 4 * sizeof(int)) != cudaSuccess) {
         kwg_destroy(ctx);
         return nullptr;
     }
@@ -274,6 +277,7 @@ void kwg_destroy(kwg_ctx* ctx)
     for (auto& e : ctx->events) {
         cudaEventDestroy(e.start);
         cudaEventDestroy(e.stop);
+        cudaFreeHost(e.bytes);
     }
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -291,18 +295,22 @@ int kwg_set_profiling(kwg_ctx* ctx, int enable)
     return KWG_OK;
 }
 
-int kwg_profile_read(kwg_ctx* ctx, double* solve_ms, int* solve_launches)
+int kwg_profile_read(kwg_ctx* ctx, double* solve_ms, int* solve_launches, double* solve_bytes)
 {
     if (!ctx) return KWG_ERR_INVALID;
-    double total = 0.;
+    double total = 0., bytes = 0.;
     for (size_t i = 0; i < ctx->events_used; ++i) {
         KWG_CUDA(ctx, cudaEventSynchronize(ctx->events[i].stop));
         float ms = 0.f;
         KWG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->events[i].start, ctx->events[i].stop));
         total += ms;
     }
+    KWG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    KWG_CUDA(ctx, cudaDeviceSynchronize());
+    for (size_t i = 0; i < ctx->events_used; ++i) bytes += (double)*ctx->events[i].bytes;
     if (solve_ms) *solve_ms = total;
     if (solve_launches) *solve_launches = (int)ctx->events_used;
+    if (solve_bytes) *solve_bytes = bytes;
     ctx->events_used = 0;
     return KWG_OK;
 }

@@ -139,7 +139,7 @@ extern "C" int kwg_fd1d_price_device_static(const kwg_option* d_opts, size_t n, 
     int8_t* w = (int8_t*)take(n);
     uint8_t* e = (uint8_t*)take(n);
     int32_t* pde_status = (int32_t*)take(m_pad * 4);
-    int* counters = (int*)take(2 * sizeof(int));
+    int* counters = (int*)take(4 * sizeof(int));
     double* rec = (double*)(s + o);
 
     cudaStream_t st = (cudaStream_t)stream;

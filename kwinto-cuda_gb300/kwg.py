@@ -84,7 +84,8 @@ def lib() -> ctypes.CDLL:
     L.kwg_fd1d_price_device.restype = i32
     L.kwg_set_profiling.argtypes = [vp, i32]
     L.kwg_set_profiling.restype = i32
-    L.kwg_profile_read.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
+    L.kwg_profile_read.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
+                                   ctypes.POINTER(ctypes.c_double)]
     L.kwg_profile_read.restype = i32
     _lib = L
     return L
@@ -125,13 +126,13 @@ class Context:
     def set_profiling(self, on: bool):
         self._L.kwg_set_profiling(self.ptr, 1 if on else 0)
 
-    def profile_read(self):
-        """(summed solve-kernel ms, launches) since the last read."""
-        ms, cnt = ctypes.c_double(0), ctypes.c_int(0)
-        rc = self._L.kwg_profile_read(self.ptr, ctypes.byref(ms), ctypes.byref(cnt))
+    def profile_read(self, with_bytes: bool = False):
+        """(summed solve-kernel ms, launches[, bytes read+written]) since the last read."""
+        ms, cnt, nb = ctypes.c_double(0), ctypes.c_int(0), ctypes.c_double(0)
+        rc = self._L.kwg_profile_read(self.ptr, ctypes.byref(ms), ctypes.byref(cnt), ctypes.byref(nb))
         if rc:
             raise RuntimeError(self.last_error())
-        return ms.value, cnt.value
+        return (ms.value, cnt.value, nb.value) if with_bytes else (ms.value, cnt.value)
 
     def fd1d_price(self, opts: np.ndarray, params: Fd1dParams):
         """Host arrays in, host arrays out. Returns (rc, prices, status)."""
