@@ -44,9 +44,10 @@ extern "C" {
 #define KWG_FP64 0 /* all stepping in FP64: parity with the reference to <= 1e-10 relative */
 #define KWG_FP32 1 /* FP32 stepping with FP64-accurate state and residual (see DESIGN) */
 
-#define KWG_SOLVER_AUTO 0
-#define KWG_SOLVER_THOMAS 1 /* thread per option, option-interleaved streaming layout */
-#define KWG_SOLVER_PCR 2    /* warp per option, partitioned solve with shuffles, state on chip */
+#define KWG_SOLVER_AUTO 0   /* the autotuned choice for this shape, else a cost model */
+#define KWG_SOLVER_THOMAS 1 /* FP64: thread per option, option-interleaved streaming layout */
+#define KWG_SOLVER_PCR 2    /* warp per option, partitioned solve with warp-shuffle cyclic
+                               reduction, state on chip (FP64: x_dim <= 1024; FP32: <= 2048) */
 
 /* Same field order, types and 56-byte layout as kw::Option (src/Core/kwAsset.h:12-22). */
 typedef struct kwg_option {
@@ -125,6 +126,14 @@ int kwg_fd1d_price_device(kwg_ctx* ctx, const kwg_option* d_opts, size_t n,
 int kwg_fd1d_price_device_static(const kwg_option* d_opts, size_t n, const kwg_fd1d_params* p,
                                  double* d_prices, int32_t* d_status, void* stream, char* err,
                                  size_t errlen);
+
+/* Autotuner.  Times the FP64 solvers -- thread per option (Thomas, 32 options per
+ * block) and warp per option (PCR, 32 threads per option) -- on a synthetic batch
+ * of m options with p's grid, and records the faster one for KWG_SOLVER_AUTO calls
+ * of the same shape (precision, x_dim, t_dim, m rounded to a power of two) on this
+ * context.  Writes each solver's solve time (ms; negative if not applicable).
+ * No counterpart in the reference, which has one CPU solver. */
+int kwg_autotune(kwg_ctx* ctx, const kwg_fd1d_params* p, size_t m, double* thomas_ms, double* pcr_ms);
 
 /* Number of kernel launches the last pricing call made (for launch accounting). */
 int kwg_last_launch_count(const kwg_ctx* ctx);

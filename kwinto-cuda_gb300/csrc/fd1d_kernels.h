@@ -67,6 +67,17 @@ int fd1d_fp32_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh
                      int* counters, double* prices, int32_t* status, int device, cudaStream_t stream,
                      const SolveEvents* ev);
 
+// FP64 warp-per-PDE on-chip solve (x_dim <= 1024).  Same work buffer as FP32.
+int fd1d_pcr64_nodes_per_lane(int x_dim);
+int fd1d_pcr64_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* vout, int32_t* pde_status,
+                      int* counters, double* prices, int32_t* status, int device, cudaStream_t stream,
+                      const SolveEvents* ev);
+
+// Interpolation over a [m][x_dim] array of final values (FP32 and PCR paths).
+__global__ void fd1d_interp_rows(const PdeBatch b, const AssetBatch a, Fd1dShape sh, const double* __restrict__ vrow,
+                                 const int32_t* __restrict__ pde_status, double* __restrict__ prices,
+                                 int32_t* __restrict__ status);
+
 // Occupancy-derived persistent grid size for the FP64 solve kernel.
 int fd1d_fp64_solve_blocks(int ntiles, int device);
 

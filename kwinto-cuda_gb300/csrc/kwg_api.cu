@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <numeric>
 #include <string>
 #include <tuple>
@@ -39,6 +40,8 @@ struct kwg_ctx {
     void* h_io = nullptr;
     size_t h_io_bytes = 0;
     // solve-kernel timing (kwg_set_profiling)
+    // autotuner decisions: shape key -> solver (KWG_SOLVER_THOMAS or KWG_SOLVER_PCR)
+    std::map<uint64_t, int> tuned;
     bool profiling = false;
     std::vector<kwg::SolveEvents> events;  // pool, reused across reads
     size_t events_used = 0;
@@ -117,8 +120,8 @@ int check_params(kwg_ctx* ctx, const kwg_fd1d_params* p)
         return set_err(ctx, KWG_ERR_INVALID, "kwg: unknown precision");
     if (p->solver < KWG_SOLVER_AUTO || p->solver > KWG_SOLVER_PCR)
         return set_err(ctx, KWG_ERR_INVALID, "kwg: unknown solver");
-    if (p->precision == KWG_FP64 && p->solver == KWG_SOLVER_PCR)
-        return set_err(ctx, KWG_ERR_INVALID, "kwg: FP64 uses the Thomas solver (KWG_SOLVER_THOMAS or AUTO)");
+    if (p->precision == KWG_FP64 && p->solver == KWG_SOLVER_PCR && kwg::fd1d_pcr64_nodes_per_lane(p->x_dim) < 0)
+        return set_err(ctx, KWG_ERR_INVALID, "kwg: the FP64 PCR solver supports x_dim <= 1024");
     if (p->precision == KWG_FP32 && p->solver == KWG_SOLVER_THOMAS)
         return set_err(ctx, KWG_ERR_INVALID, "kwg: FP32 uses the on-chip partitioned solver (KWG_SOLVER_PCR or AUTO)");
     if (p->precision == KWG_FP32 && kwg::fd1d_fp32_nodes_per_lane(p->x_dim) < 0)
@@ -191,6 +194,28 @@ __global__ void unpack_options(const kwg_option* __restrict__ o, int n, double* 
     e[i] = a.e;
 }
 
+uint64_t shape_key(int precision, int x_dim, int t_dim, int m)
+{
+    int mb = 0;
+    while ((1 << mb) < m && mb < 40) ++mb;
+    return ((uint64_t)precision << 60) | ((uint64_t)(x_dim & 0xfffff) << 40) | ((uint64_t)(t_dim & 0xfffff) << 20) |
+           (uint64_t)mb;
+}
+
+// Solver for an FP64 batch: explicit choice, the autotuned one, else a cost model.
+// The thread-per-option kernel runs m/32 warps; the warp-per-option kernel runs m
+// warps at twice the FP64 work per node-step, so it wins while m/32 warps cannot
+// fill the GPU (a few warps per SM).
+int choose_solver(kwg_ctx* ctx, const kwg_fd1d_params* p, int m)
+{
+    if (p->precision == KWG_FP32) return KWG_SOLVER_PCR;
+    if (p->solver != KWG_SOLVER_AUTO) return p->solver;
+    const bool pcr_ok = kwg::fd1d_pcr64_nodes_per_lane(p->x_dim) > 0;
+    auto it = ctx->tuned.find(shape_key(p->precision, p->x_dim, p->t_dim, m));
+    if (it != ctx->tuned.end()) return it->second;
+    return (pcr_ok && m < 8192) ? KWG_SOLVER_PCR : KWG_SOLVER_THOMAS;
+}
+
 int run_batch(kwg_ctx* ctx, char* io, const IoLayout& L, int m, int n, const kwg_fd1d_params* p,
               double* prices, int32_t* status, cudaStream_t stream)
 {
@@ -211,7 +236,16 @@ int run_batch(kwg_ctx* ctx, char* io, const IoLayout& L, int m, int n, const kwg
     a.n = n;
     const kwg::Fd1dShape sh = make_shape(p);
 
-    if (p->precision == KWG_FP32) {
+    const int solver = choose_solver(ctx, p, m);
+    if (p->precision == KWG_FP64 && solver == KWG_SOLVER_PCR) {
+        const size_t wbytes = kwg::fd1d_fp32_work_bytes(m, sh.x_dim);
+        if (int rc = ensure_device(ctx, &ctx->d_work, &ctx->work_bytes, wbytes)) return rc;
+        const int n_launch = kwg::fd1d_pcr64_launch(b, a, sh, (double*)ctx->d_work, (int32_t*)(io + L.pde_status),
+                                                    ctx->d_counter, prices, status, ctx->device, stream,
+                                                    ctx->next_events());
+        if (n_launch < 0) return set_err(ctx, KWG_ERR_INVALID, "kwg: the FP64 PCR solver supports x_dim <= 1024");
+        ctx->launches += n_launch;
+    } else if (p->precision == KWG_FP32) {
         const size_t wbytes = kwg::fd1d_fp32_work_bytes(m, sh.x_dim);
         if (int rc = ensure_device(ctx, &ctx->d_work, &ctx->work_bytes, wbytes)) return rc;
         const int n_launch = kwg::fd1d_fp32_launch(b, a, sh, (double*)ctx->d_work, (int32_t*)(io + L.pde_status),
@@ -402,6 +436,50 @@ int kwg_fd1d_price(kwg_ctx* ctx, const kwg_option* opts, size_t n, const kwg_fd1
             return set_err(ctx, hs[i] == KWG_STATUS_SOLVER ? KWG_ERR_SOLVER : KWG_ERR_INVALID, msg);
         }
     }
+    return KWG_OK;
+}
+
+int kwg_autotune(kwg_ctx* ctx, const kwg_fd1d_params* p, size_t m, double* thomas_ms, double* pcr_ms)
+{
+    if (!ctx) return KWG_ERR_INVALID;
+    ctx->err.clear();
+    if (int rc = check_params(ctx, p)) return rc;
+    if (thomas_ms) *thomas_ms = -1.;
+    if (pcr_ms) *pcr_ms = -1.;
+    if (m == 0 || m > (size_t)INT32_MAX / 2) return set_err(ctx, KWG_ERR_INVALID, "kwg_autotune: bad batch size");
+    if (p->precision != KWG_FP64) return KWG_OK;  // FP32 has one solver
+    // synthetic batch: puts and calls, strikes 80..120, vols 0.1..0.6, maturities 0.25..2
+    std::vector<kwg_option> opts(m);
+    for (size_t i = 0; i < m; ++i) {
+        const double u = (double)((i * 2654435761u) % 1000) / 1000.;
+        const double v = (double)((i * 40503u + 17) % 997) / 997.;
+        opts[i] = kwg_option{0.25 + 1.75 * v, 80. + 40. * u, 0.1 + 0.5 * (1. - u), 0.05, 0.02, 100., 1,
+                             (int8_t)((i & 1) ? 1 : -1)};
+    }
+    kwg_fd1d_params q = *p;
+    q.strict = 0;
+    std::vector<double> prices(m);
+    const bool was_profiling = ctx->profiling;
+    double best_ms[3] = {-1., -1., -1.};
+    for (int solver : {KWG_SOLVER_THOMAS, KWG_SOLVER_PCR}) {
+        if (solver == KWG_SOLVER_PCR && kwg::fd1d_pcr64_nodes_per_lane(p->x_dim) < 0) continue;
+        q.solver = solver;
+        if (int rc = kwg_fd1d_price(ctx, opts.data(), m, &q, prices.data(), nullptr)) return rc;  // warm-up
+        kwg_set_profiling(ctx, 1);
+        int rc = kwg_fd1d_price(ctx, opts.data(), m, &q, prices.data(), nullptr);
+        double ms = 0.;
+        int cnt = 0;
+        if (!rc) rc = kwg_profile_read(ctx, &ms, &cnt, nullptr);
+        kwg_set_profiling(ctx, was_profiling);
+        if (rc) return rc;
+        best_ms[solver] = ms;
+    }
+    if (thomas_ms) *thomas_ms = best_ms[KWG_SOLVER_THOMAS];
+    if (pcr_ms) *pcr_ms = best_ms[KWG_SOLVER_PCR];
+    const int pick = (best_ms[KWG_SOLVER_PCR] >= 0. && best_ms[KWG_SOLVER_PCR] < best_ms[KWG_SOLVER_THOMAS])
+                         ? KWG_SOLVER_PCR
+                         : KWG_SOLVER_THOMAS;
+    ctx->tuned[shape_key(p->precision, p->x_dim, p->t_dim, (int)m)] = pick;
     return KWG_OK;
 }
 

@@ -82,6 +82,9 @@ def lib() -> ctypes.CDLL:
     L.kwg_fd1d_price.restype = i32
     L.kwg_fd1d_price_device.argtypes = [vp, vp, sz, ctypes.POINTER(Fd1dParams), dp, dp, vp]
     L.kwg_fd1d_price_device.restype = i32
+    L.kwg_autotune.argtypes = [vp, ctypes.POINTER(Fd1dParams), sz, ctypes.POINTER(ctypes.c_double),
+                               ctypes.POINTER(ctypes.c_double)]
+    L.kwg_autotune.restype = i32
     L.kwg_set_profiling.argtypes = [vp, i32]
     L.kwg_set_profiling.restype = i32
     L.kwg_profile_read.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
@@ -133,6 +136,15 @@ class Context:
         if rc:
             raise RuntimeError(self.last_error())
         return (ms.value, cnt.value, nb.value) if with_bytes else (ms.value, cnt.value)
+
+    def autotune(self, params: Fd1dParams, m: int):
+        """Times the FP64 solvers on a synthetic batch of m options; records the faster
+        one for KWG_SOLVER_AUTO.  Returns (thomas_ms, pcr_ms); -1 if not applicable."""
+        a, b = ctypes.c_double(0), ctypes.c_double(0)
+        rc = self._L.kwg_autotune(self.ptr, ctypes.byref(params), m, ctypes.byref(a), ctypes.byref(b))
+        if rc:
+            raise RuntimeError(self.last_error())
+        return a.value, b.value
 
     def fd1d_price(self, opts: np.ndarray, params: Fd1dParams):
         """Host arrays in, host arrays out. Returns (rc, prices, status)."""

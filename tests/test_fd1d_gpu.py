@@ -1,5 +1,6 @@
 """GPU parity of the FP64 FD1D path against the oracle and the reference's golden
-vectors, through the C ABI.  Tolerance: the FP64 path must match the reference to
+vectors, through the C ABI, for both FP64 solvers (thread-per-option Thomas and
+warp-per-option PCR).  Tolerance: the FP64 path must match the reference to
 REL_TOL = 1e-10 relative on every option."""
 import math
 
@@ -27,38 +28,45 @@ def gpu_price(ctx, opts, **kw):
     return p, st
 
 
-def test_pricer_test_table(ctx):
+SOLVERS = pytest.mark.parametrize("solver", [1, 2], ids=["thomas", "pcr"])
+
+
+@SOLVERS
+def test_pricer_test_table(ctx, solver):
     """test/kwPricer_test.cpp:63-84 at the reference defaults (512x512, scale 50, d 0.25)."""
     g = golden("pricer_test.npz")
-    p, st = gpu_price(ctx, g["opts"])
+    p, st = gpu_price(ctx, g["opts"], solver=solver)
     assert (st == 0).all()
     assert rel_err(p, g["ref_fd1d"]) <= REL_TOL
     assert np.max(np.abs(p - g["want"])) <= 1.3e-3
 
 
+@SOLVERS
 @pytest.mark.parametrize("name", ["qdfp", "fd1d"])
-def test_portfolio_fixtures(ctx, name):
+def test_portfolio_fixtures(ctx, name, solver):
     """test/kwPortfolio_test.cpp:41-56: 6000 puts, 600 distinct PDEs (dedup path)."""
     g = golden(f"portfolio_{name}.npz")
-    p, st = gpu_price(ctx, g["opts"], t_dim=512, x_dim=512)
+    p, st = gpu_price(ctx, g["opts"], t_dim=512, x_dim=512, solver=solver)
     assert (st == 0).all()
     assert rel_err(p, g["ref_fd1d"]) <= REL_TOL
     if name == "qdfp":
         assert np.max(np.abs(p - g["quantlib"])) <= 0.005
 
 
-def test_config1(ctx):
+@SOLVERS
+def test_config1(ctx, solver):
     g = golden("synthetic.npz")
-    p, st = gpu_price(ctx, g["config1_opts"], t_dim=512, x_dim=512, scale=5.0, density=0.25)
+    p, st = gpu_price(ctx, g["config1_opts"], t_dim=512, x_dim=512, scale=5.0, density=0.25, solver=solver)
     assert (st == 0).all() and rel_err(p, g["config1_ref"]) <= REL_TOL
 
 
-def test_config2_sample_sinh_and_uniform(ctx):
+@SOLVERS
+def test_config2_sample_sinh_and_uniform(ctx, solver):
     """1024x1024: the reference at density 1e6, the GPU both at 1e6 and exactly uniform."""
     g = golden("synthetic.npz")
-    p, _ = gpu_price(ctx, g["config2_opts"], t_dim=1024, x_dim=1024, scale=5.0, density=1e6)
+    p, _ = gpu_price(ctx, g["config2_opts"], t_dim=1024, x_dim=1024, scale=5.0, density=1e6, solver=solver)
     assert rel_err(p, g["config2_ref"]) <= REL_TOL
-    u, _ = gpu_price(ctx, g["config2_opts"], t_dim=1024, x_dim=1024, scale=5.0, density=math.inf)
+    u, _ = gpu_price(ctx, g["config2_opts"], t_dim=1024, x_dim=1024, scale=5.0, density=math.inf, solver=solver)
     assert rel_err(u, g["config2_ref"]) <= REL_TOL
 
 
@@ -68,12 +76,13 @@ def test_config4_sample(ctx):
     assert rel_err(p, g["config4_ref"]) <= REL_TOL
 
 
+@SOLVERS
 @pytest.mark.parametrize("name,kw", [("default", {}), ("x3_t2", dict(x_dim=3, t_dim=2)),
                                      ("x7_t5", dict(x_dim=7, t_dim=5)),
                                      ("x64_t33", dict(x_dim=64, t_dim=33, scale=5.0))])
-def test_edge_grids_european_calls_duplicates(ctx, name, kw):
+def test_edge_grids_european_calls_duplicates(ctx, name, kw, solver):
     g = golden("edge.npz")
-    p, st = gpu_price(ctx, g["opts"], **kw)
+    p, st = gpu_price(ctx, g["opts"], solver=solver, **kw)
     assert (st == 0).all() and rel_err(p, g[f"ref_{name}"]) <= REL_TOL
 
 
@@ -89,26 +98,28 @@ def test_out_of_grid_status_and_strict(ctx):
     assert rc == kwg.KWG_ERR_OUT_OF_GRID and "not in grid range" in ctx.last_error()
 
 
+@SOLVERS
 @pytest.mark.parametrize("theta", [0.6, 0.75, 1.0])
-def test_theta_other_than_half(ctx, theta):
+def test_theta_other_than_half(ctx, theta, solver):
     """theta is hard-coded to 0.5 in the reference; other values follow the oracle."""
     import kwor
 
     o = golden("synthetic.npz")["config1_opts"][:40]
-    p, _ = gpu_price(ctx, o, t_dim=200, x_dim=160, scale=5.0, density=0.25, theta=theta)
+    p, _ = gpu_price(ctx, o, t_dim=200, x_dim=160, scale=5.0, density=0.25, theta=theta, solver=solver)
     rc, msg, want, _ = kwor.fd1d_price(o, t_dim=200, x_dim=160, scale=5.0, density=0.25, theta=theta)
     assert rc == 0, msg
     assert rel_err(p, want) <= REL_TOL
 
 
+@SOLVERS
 @pytest.mark.parametrize("n", [1, 31, 33, 100])
-def test_ragged_batches(ctx, n):
-    """PDE counts that are not a multiple of the 32-lane tile."""
+def test_ragged_batches(ctx, n, solver):
+    """PDE counts that are not a multiple of the 32-lane tile; x_dim not a power of 2."""
     import kwor
     import portfolio
 
     o = portfolio.config1_like(n, seed=99)
-    p, st = gpu_price(ctx, o, t_dim=64, x_dim=96, scale=5.0, density=0.25)
+    p, st = gpu_price(ctx, o, t_dim=64, x_dim=96, scale=5.0, density=0.25, solver=solver)
     rc, msg, want, _ = kwor.fd1d_price(o, t_dim=64, x_dim=96, scale=5.0, density=0.25)
     assert (st == 0).all() and rel_err(p, want) <= REL_TOL
 
@@ -120,20 +131,21 @@ def test_empty_batch_and_invalid_params(ctx):
     assert rc == kwg.KWG_OK and len(p) == 0
     o = golden("edge.npz")["opts"]
     for bad in (dict(x_dim=2), dict(t_dim=1), dict(theta=0.0), dict(theta=1.5), dict(scale=-1.0),
-                dict(density=0.0)):
+                dict(density=0.0), dict(solver=2, x_dim=2048)):
         rc, _, _ = ctx.fd1d_price(o, kwg.params(**bad))
         assert rc == kwg.KWG_ERR_INVALID, bad
         assert ctx.last_error().startswith("kwg:")
 
 
-def test_bad_option_fields(ctx):
+@SOLVERS
+def test_bad_option_fields(ctx, solver):
     import kwg
 
     o = golden("edge.npz")["opts"].copy()
     o[1]["t"] = 0.0
     o[5]["z"] = -0.2
     o[7]["s"] = 0.0
-    p, st = gpu_price(ctx, o)
+    p, st = gpu_price(ctx, o, solver=solver)
     assert st[1] == kwg.STATUS_BAD_INPUT and st[5] == kwg.STATUS_BAD_INPUT and st[7] == kwg.STATUS_BAD_INPUT
     assert np.isnan(p[[1, 5, 7]]).all()
     assert (st[[0, 2, 3, 4, 6]] == 0).all()
@@ -198,3 +210,22 @@ def test_config2_full_size_properties(ctx):
     idx = np.arange(0, 32768, 1024)
     rc, msg, want, _ = kwor.fd1d_price(o[idx], t_dim=1024, x_dim=1024, scale=5.0, density=math.inf)
     assert rc == 0 and rel_err(p[idx], want) <= REL_TOL
+
+
+def test_solvers_agree_and_autotune(ctx):
+    """Both FP64 solvers give the same prices to 1e-10; the autotuner times both and
+    AUTO then matches them too."""
+    import kwg
+    import portfolio
+
+    o = portfolio.config1_like(777, seed=17)
+    kw = dict(t_dim=300, x_dim=256, scale=5.0, density=0.25)
+    a, _ = gpu_price(ctx, o, solver=kwg.SOLVER_THOMAS, **kw)
+    b, _ = gpu_price(ctx, o, solver=kwg.SOLVER_PCR, **kw)
+    assert rel_err(b, a) <= REL_TOL
+    t_ms, p_ms = ctx.autotune(kwg.params(**kw), len(o))
+    assert t_ms > 0 and p_ms > 0
+    c, _ = gpu_price(ctx, o, **kw)
+    assert rel_err(c, a) <= REL_TOL
+    t_ms, p_ms = ctx.autotune(kwg.params(t_dim=64, x_dim=2048, scale=5.0), 64)
+    assert t_ms > 0 and p_ms < 0  # PCR-FP64 stops at x_dim 1024
