@@ -127,6 +127,18 @@ int kwg_fd1d_price_device_static(const kwg_option* d_opts, size_t n, const kwg_f
                                  double* d_prices, int32_t* d_status, void* stream, char* err,
                                  size_t errlen);
 
+/* Prices n options in HOST memory, option i on its own grid of x_dims[i] nodes and
+ * t_dims[i] time levels (p's x_dim and t_dim are ignored; its other fields apply).
+ * The reference prices one grid shape per Fd1d_Pricer::init
+ * (src/Pricer/kwFd1d.cpp:15-16), so a mixed portfolio needs one reference call per
+ * shape; here the whole batch is one persistent launch (FP64 Thomas) or one launch
+ * per nodes-per-lane bucket (PCR and FP32), replayed from a CUDA graph while the
+ * batch layout is unchanged.  Dedup key: (t, r, q, z, e, w, x_dim, t_dim).
+ * Results and status as kwg_fd1d_price.  Blocking. */
+int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const int32_t* x_dims,
+                          const int32_t* t_dims, size_t n, const kwg_fd1d_params* p,
+                          double* prices, int32_t* status);
+
 /* Autotuner.  Times the FP64 solvers -- thread per option (Thomas, 32 options per
  * block) and warp per option (PCR, 32 threads per option) -- on a synthetic batch
  * of m options with p's grid, and records the faster one for KWG_SOLVER_AUTO calls

@@ -71,7 +71,6 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
     extern __shared__ float tab[];  // [M][kF32Fields][32]
     const int k = threadIdx.x & 31;
     auto T = [&](int i, int f) -> float& { return tab[(i * kF32Fields + f) * 32 + k]; };
-    const int N = sh.x_dim;
     const int j0 = k * M;
 
     for (;;) {
@@ -79,6 +78,8 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
         if (k == 0) pde = atomicAdd(&counters[0], 1);
         pde = __shfl_sync(kFull, pde, 0);
         if (pde >= b.m) break;
+        const int N = shape_x(sh, pde);
+        const int TL = shape_t(sh, pde);  // time levels of this PDE
 
         // ------------------------------------------------------------ setup
         const double t = b.t[pde], z = b.z[pde], rr = b.r[pde], qq = b.q[pde];
@@ -90,7 +91,7 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
         Grid g;
         g.init(z, t, sh.scale, sh.density, N, sh.uniform);
         const Coef a = pde_coef(rr, qq, z);
-        const double dt = time_step(t, sh.t_dim);
+        const double dt = time_step(t, TL);
 
         // One FP64 pass over this lane's nodes: grid, operator row, residual
         // coefficients, payoff, and the LU of the interior block B_I with the four
@@ -253,7 +254,7 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
         }
 
         // ------------------------------------------------------------ time steps
-        for (int step = 1; run && step < sh.t_dim; ++step) {
+        for (int step = 1; run && step < TL; ++step) {
             float Hm = __shfl_up_sync(kFull, H[M - 1], 1), Lm = __shfl_up_sync(kFull, Lo[M - 1], 1);
             float Hp = __shfl_down_sync(kFull, H[0], 1), Lp = __shfl_down_sync(kFull, Lo[0], 1);
             if (k == 0) Hm = Lm = 0.f;
@@ -313,7 +314,7 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
             }
         }
         // ------------------------------------------------------------ result
-        double* V = vout + (size_t)pde * N;
+        double* V = vout + shape_row(sh, pde);
 #pragma unroll
         for (int i = 0; i < M; ++i)
             if (j0 + i < N) V[j0 + i] = (double)H[i] + (double)Lo[i];
@@ -329,7 +330,7 @@ __global__ void fd1d_interp_rows(const PdeBatch b, const AssetBatch a, Fd1dShape
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const int slot = a.pde[i];
-    const int N = sh.x_dim;
+    const int N = shape_x(sh, slot);
     const double s = a.s[i], k = a.k[i];
     int32_t st = pde_status[slot];
     if (!(s > 0.) || !(k > 0.) || !isfinite(s) || !isfinite(k)) st = KWG_STATUS_BAD_INPUT;
@@ -349,7 +350,7 @@ __global__ void fd1d_interp_rows(const PdeBatch b, const AssetBatch a, Fd1dShape
         if (lo == 0 || lo == N) {
             st = KWG_STATUS_OUT_OF_GRID;
         } else {
-            const double* V = vrow + (size_t)slot * N;
+            const double* V = vrow + shape_row(sh, slot);
             const double xl = g.x(lo - 1), xh = g.x(lo);
             const double v = dvd(add(mul(sub(xh, xs), V[lo - 1]), mul(sub(xs, xl), V[lo])), sub(xh, xl));
             price = mul(k, v);
@@ -361,15 +362,30 @@ __global__ void fd1d_interp_rows(const PdeBatch b, const AssetBatch a, Fd1dShape
 
 namespace {
 
+// Resident blocks per SM of fd1d_solve_fp32<M>, set by fd1d_fp32_prepare.
 template <int M>
-int launch_m(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* vout, int32_t* pde_status,
-             int* counters, double* prices, int32_t* status, int sms, cudaStream_t stream, const SolveEvents* ev)
+int& per_sm_fp32()
+{
+    static int v = 1;
+    return v;
+}
+
+template <int M>
+void prepare_m()
 {
     const size_t smem = (size_t)M * kF32Fields * 32 * sizeof(float);
     cudaFuncSetAttribute(fd1d_solve_fp32<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fd1d_solve_fp32<M>, 32, smem);
-    if (per_sm < 1) per_sm = 1;
+    per_sm_fp32<M>() = per_sm < 1 ? 1 : per_sm;
+}
+
+template <int M>
+int launch_m(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* vout, int32_t* pde_status,
+             int* counters, double* prices, int32_t* status, int sms, cudaStream_t stream, const SolveEvents* ev)
+{
+    const size_t smem = (size_t)M * kF32Fields * 32 * sizeof(float);
+    const int per_sm = per_sm_fp32<M>();
     const int blocks = b.m < sms * per_sm ? b.m : sms * per_sm;
     cudaMemsetAsync(counters, 0, 4 * sizeof(int), stream);
     if (ev) cudaEventRecord(ev->start, stream);
@@ -384,6 +400,16 @@ int launch_m(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double
 }
 
 }  // namespace
+
+void fd1d_fp32_prepare(int)
+{
+    prepare_m<2>();
+    prepare_m<4>();
+    prepare_m<8>();
+    prepare_m<16>();
+    prepare_m<32>();
+    prepare_m<64>();
+}
 
 int fd1d_fp32_nodes_per_lane(int x_dim)
 {

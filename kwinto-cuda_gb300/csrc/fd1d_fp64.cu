@@ -70,9 +70,9 @@ struct Work {
     int2* range;  // [m_pad]: first and last node of the middle region (empty: x > y)
 };
 
-__device__ __forceinline__ Work work_of(double* base, int m_pad, int n)
+__device__ __forceinline__ Work work_of(double* base, int m_pad, long long node_lanes)
 {
-    const size_t nodes = (size_t)m_pad * n;
+    const size_t nodes = (size_t)node_lanes;
     Work w;
     w.cu = base;
     w.cd = w.cu + nodes * kCoef;
@@ -91,10 +91,22 @@ struct TileView {
     double* s;
 };
 
-__device__ __forceinline__ TileView tile_view(const Work& w, int tile, int n)
+// Node count and first node-lane of a tile (uniform batches: all tiles alike).
+__device__ __forceinline__ void tile_shape(const Fd1dShape& sh, int tile, int& n, long long& off)
+{
+    if (sh.tiles) {
+        n = sh.tiles[tile].n;
+        off = sh.tiles[tile].off;
+    } else {
+        n = sh.x_dim;
+        off = (long long)tile * sh.x_dim * kTile;
+    }
+}
+
+__device__ __forceinline__ TileView tile_view(const Work& w, long long off)
 {
     TileView v;
-    const size_t base = (size_t)tile * n * kTile;
+    const size_t base = (size_t)off;
     v.cu = w.cu + base * kCoef;
     v.cd = w.cd + base * kCoef;
     v.p = w.p + base;
@@ -118,9 +130,11 @@ __global__ void __launch_bounds__(128) fd1d_setup_fp64(const PdeBatch b, Fd1dSha
     if (slot >= b.m_pad) return;
     const int src = slot < b.m ? slot : b.m - 1;  // padding lanes replicate the last PDE
     const int tile = slot / kTile, lane = slot % kTile;
-    const int N = sh.x_dim;
-    const Work wk = work_of(base, b.m_pad, N);
-    const TileView tv = tile_view(wk, tile, N);
+    int N;
+    long long toff;
+    tile_shape(sh, tile, N, toff);
+    const Work wk = work_of(base, b.m_pad, sh.node_lanes);
+    const TileView tv = tile_view(wk, toff);
     auto CU = [&](int j, int f) -> double& { return tv.cu[((size_t)j * kCoef + f) * kTile + lane]; };
     auto CD = [&](int j, int f) -> double& { return tv.cd[((size_t)j * kCoef + f) * kTile + lane]; };
     auto P = [&](int j) -> double& { return tv.p[(size_t)j * kTile + lane]; };
@@ -136,7 +150,7 @@ __global__ void __launch_bounds__(128) fd1d_setup_fp64(const PdeBatch b, Fd1dSha
     Grid g;
     g.init(z, t, sh.scale, sh.density, N, sh.uniform);
     const Coef a = pde_coef(b.r[src], b.q[src], z);
-    const double dt = time_step(t, sh.t_dim);
+    const double dt = time_step(t, shape_t(sh, src));
     const double theta = sh.theta;
     // uniform grids: rows from the exact spacing, so interior rows are identical
     const double hx = sh.uniform ? dvd(sub(g.xMax, g.xMin), (double)(N - 1)) : 0.;
@@ -303,7 +317,7 @@ __device__ void drain(const Ring& r, uint32_t from, uint32_t to)
 // One sweep over this warp's tile.  Returns false on a wait timeout (already drained).
 template <bool kUp, bool kHalf>
 __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileView& tv, int lane, int N, int lo,
-                                      int hi, const double* cst, double c, bool amer, int* err)
+                                      int hi, const double* cst, double c, bool amer, bool active, int* err)
 {
     const int ng = (N + kGroup - 1) / kGroup;
     const int pre = ng < kRing ? ng : kRing;
@@ -359,7 +373,7 @@ __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileVi
                 double vn = kHalf ? fma(rs[k], yh, -rv[k]) : fma(rs[k], yh, -c * rv[k]);
                 if (amer && j < N - 1) vn = max_floor(vn, rp[k]);
                 f = fma(-rb[k], f, vn);
-                sout[(size_t)j * kTile] = make_double2(vn, f);
+                if (active) sout[(size_t)j * kTile] = make_double2(vn, f);
             }
         }
     }
@@ -392,10 +406,8 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64(const PdeBatch b, Fd1dShap
     }
     __syncwarp();
 
-    const int N = sh.x_dim;
-    const int ng = (N + kGroup - 1) / kGroup;
     const int ntiles = b.m_pad / kTile;
-    const Work wk = work_of(base, b.m_pad, N);
+    const Work wk = work_of(base, b.m_pad, sh.node_lanes);
     uint32_t q = 0;  // stage visits consumed so far
     for (;;) {
         int tile = 0;
@@ -405,7 +417,14 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64(const PdeBatch b, Fd1dShap
         const int slot = tile * kTile + lane;
         const int src = slot < b.m ? slot : b.m - 1;
         const bool amer = b.e[src] != 0;
-        const TileView tv = tile_view(wk, tile, N);
+        int N;
+        long long toff;
+        tile_shape(sh, tile, N, toff);
+        const int ng = (N + kGroup - 1) / kGroup;
+        const TileView tv = tile_view(wk, toff);
+        // every lane steps its own PDE tDim-1 times; the tile runs for its longest
+        const int t_lane = shape_t(sh, src);
+        const int t_max = sh.tiles ? sh.tiles[tile].t_max : sh.t_dim;
         // the tile's middle region is where every lane's coefficients are frozen
         const int2 rg = wk.range[slot];
         const int lo = __reduce_max_sync(0xffffffffu, rg.x);
@@ -425,14 +444,15 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64(const PdeBatch b, Fd1dShap
                 per_dn += count * (kNodePBytes + 2 * kNodeSBytes) +
                           (stage_compact(first, count, lo, hi) ? 0 : count * kNodeCoefBytes);
             }
-            const unsigned long long n_up = (unsigned long long)(sh.t_dim / 2);  // passes 1, 3, 5, ...
-            const unsigned long long n_dn = (unsigned long long)((sh.t_dim - 1) / 2);
+            const unsigned long long n_up = (unsigned long long)(t_max / 2);  // passes 1, 3, 5, ...
+            const unsigned long long n_dn = (unsigned long long)((t_max - 1) / 2);
             atomicAdd(reinterpret_cast<unsigned long long*>(tile_counter + 2), per_up * n_up + per_dn * n_dn);
         }
-        for (int pass = 1; pass < sh.t_dim; ++pass) {
-            const bool ok = (pass & 1) ? sweep<true, kHalf>(ring, q, tv, lane, N, lo, hi, cst, sh.c, amer,
+        for (int pass = 1; pass < t_max; ++pass) {
+            const bool act = pass < t_lane;
+            const bool ok = (pass & 1) ? sweep<true, kHalf>(ring, q, tv, lane, N, lo, hi, cst, sh.c, amer, act,
                                                             &tile_counter[1])
-                                       : sweep<false, kHalf>(ring, q, tv, lane, N, lo, hi, cst, sh.c, amer,
+                                       : sweep<false, kHalf>(ring, q, tv, lane, N, lo, hi, cst, sh.c, amer, act,
                                                              &tile_counter[1]);
             if (!ok) return;
             q += ng;
@@ -450,7 +470,9 @@ __global__ void fd1d_interp_fp64(const PdeBatch b, const AssetBatch a, Fd1dShape
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const int slot = a.pde[i];
-    const int N = sh.x_dim;
+    int N;
+    long long toff;
+    tile_shape(sh, slot / kTile, N, toff);
     const double s = a.s[i], k = a.k[i];
     int32_t st = pde_status[slot];
     if (*device_error) st = KWG_STATUS_DEVICE_TIMEOUT;
@@ -471,7 +493,7 @@ __global__ void fd1d_interp_fp64(const PdeBatch b, const AssetBatch a, Fd1dShape
         if (lo == 0 || lo == N) {
             st = KWG_STATUS_OUT_OF_GRID;
         } else {
-            const TileView tv = tile_view(work_of(base, b.m_pad, N), slot / kTile, N);
+            const TileView tv = tile_view(work_of(base, b.m_pad, sh.node_lanes), toff);
             const int lane = slot % kTile;
             const double xl = g.x(lo - 1), xh = g.x(lo);
             const double vl = tv.s[((size_t)(lo - 1) * kTile + lane) * 2];
@@ -498,16 +520,30 @@ int fd1d_fp64_solve_blocks(int ntiles, int device)
     return ntiles < cap ? (ntiles > 0 ? ntiles : 1) : cap;
 }
 
-size_t fd1d_fp64_work_bytes(int m_pad, int x_dim)
+void fd1d_prepare_kernels(int device)
 {
-    return (size_t)m_pad * x_dim * (2 * kCoef + 1 + 2) * sizeof(double) + (size_t)m_pad * kConsts * sizeof(double) +
+    static bool done[64] = {};
+    if (device < 0 || device >= 64 || done[device]) return;
+    fd1d_fp64_solve_blocks(1, device);  // caches the FP64 kernel's occupancy
+    fd1d_fp32_prepare(device);
+    fd1d_pcr64_prepare(device);
+    done[device] = true;
+}
+
+size_t fd1d_fp64_work_bytes_nl(int m_pad, long long node_lanes)
+{
+    return (size_t)node_lanes * (2 * kCoef + 1 + 2) * sizeof(double) + (size_t)m_pad * kConsts * sizeof(double) +
            (size_t)m_pad * sizeof(int2);
 }
 
-int fd1d_fp64_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* work, int32_t* pde_status,
+size_t fd1d_fp64_work_bytes(int m_pad, int x_dim) { return fd1d_fp64_work_bytes_nl(m_pad, (long long)m_pad * x_dim); }
+
+int fd1d_fp64_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh_in, double* work, int32_t* pde_status,
                      int* counters, double* prices, int32_t* status, int solve_blocks, cudaStream_t stream,
                      const SolveEvents* ev)
 {
+    Fd1dShape sh = sh_in;
+    if (!sh.tiles) sh.node_lanes = (long long)b.m_pad * sh.x_dim;
     int launches = 0;
     fd1d_setup_fp64<<<(b.m_pad + 127) / 128, 128, 0, stream>>>(b, sh, work, pde_status);
     ++launches;

@@ -31,7 +31,17 @@ struct AssetBatch {
     int n;
 };
 
-// Grid shape and scheme parameters shared by a batch.
+// Thomas-kernel tile of an uneven batch: 32 PDE slots sharing one node count.
+struct TileDesc {
+    int n;          // nodes of every PDE in the tile
+    int t_max;      // largest time-level count among the tile's PDEs
+    long long off;  // offset of the tile's first node-lane (arrays hold node-lanes)
+};
+
+// Grid shape and scheme parameters shared by a batch.  A uniform batch uses x_dim
+// and t_dim; an uneven batch gives every PDE slot its own node count (pde_x) and
+// time levels (pde_t), and the layout of its work arrays (tiles for the Thomas
+// kernel, row_off for the kernels that write one row of final values per PDE).
 struct Fd1dShape {
     int x_dim;
     int t_dim;
@@ -40,10 +50,24 @@ struct Fd1dShape {
     double scale;
     double density;
     bool uniform;
+    const int32_t* pde_x = nullptr;
+    const int32_t* pde_t = nullptr;
+    const TileDesc* tiles = nullptr;
+    const long long* row_off = nullptr;
+    long long node_lanes = 0;  // Thomas work arrays: sum over tiles of 32 * n
 };
 
-// Device bytes of the node records of a batch (coefficients + state).
+__host__ __device__ inline int shape_x(const Fd1dShape& sh, int pde) { return sh.pde_x ? sh.pde_x[pde] : sh.x_dim; }
+__host__ __device__ inline int shape_t(const Fd1dShape& sh, int pde) { return sh.pde_t ? sh.pde_t[pde] : sh.t_dim; }
+__host__ __device__ inline long long shape_row(const Fd1dShape& sh, int pde)
+{
+    return sh.row_off ? sh.row_off[pde] : (long long)pde * sh.x_dim;
+}
+
+// Device bytes of the FP64 Thomas work arrays of a uniform batch (coefficients +
+// state), and of an uneven batch with the given node-lane count.
 size_t fd1d_fp64_work_bytes(int m_pad, int x_dim);
+size_t fd1d_fp64_work_bytes_nl(int m_pad, long long node_lanes);
 
 // Optional CUDA events recorded immediately before and after the solve kernel.
 struct SolveEvents {
@@ -77,6 +101,12 @@ int fd1d_pcr64_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& s
 __global__ void fd1d_interp_rows(const PdeBatch b, const AssetBatch a, Fd1dShape sh, const double* __restrict__ vrow,
                                  const int32_t* __restrict__ pde_status, double* __restrict__ prices,
                                  int32_t* __restrict__ status);
+
+// One-time per-device set-up of every kernel's shared-memory limit and occupancy, so
+// that launches (also inside a stream capture) make no attribute calls.
+void fd1d_prepare_kernels(int device);
+void fd1d_fp32_prepare(int device);
+void fd1d_pcr64_prepare(int device);
 
 // Occupancy-derived persistent grid size for the FP64 solve kernel.
 int fd1d_fp64_solve_blocks(int ntiles, int device);

@@ -41,7 +41,6 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64_pcr(const PdeBatch b, Fd1d
     extern __shared__ double qtab[];  // [M][kP64Fields][32]
     const int k = threadIdx.x & 31;
     auto Q = [&](int i, int f) -> double& { return qtab[(i * kP64Fields + f) * 32 + k]; };
-    const int N = sh.x_dim;
     const int j0 = k * M;
 
     for (;;) {
@@ -49,6 +48,8 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64_pcr(const PdeBatch b, Fd1d
         if (k == 0) pde = atomicAdd(&counters[0], 1);
         pde = __shfl_sync(kFull64, pde, 0);
         if (pde >= b.m) break;
+        const int N = shape_x(sh, pde);
+        const int T = shape_t(sh, pde);
 
         // ------------------------------------------------------------ setup (FP64)
         const double t = b.t[pde], z = b.z[pde], rr = b.r[pde], qq = b.q[pde];
@@ -60,7 +61,7 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64_pcr(const PdeBatch b, Fd1d
         Grid g;
         g.init(z, t, sh.scale, sh.density, N, sh.uniform);
         const Coef a = pde_coef(rr, qq, z);
-        const double dt = time_step(t, sh.t_dim);
+        const double dt = time_step(t, T);
         const double hx = sh.uniform ? dvd(sub(g.xMax, g.xMin), (double)(N - 1)) : 0.;
 
         // rows of T = theta B for this lane's nodes; interior LU as we go
@@ -173,7 +174,7 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64_pcr(const PdeBatch b, Fd1d
         for (int i = 0; i < M; ++i) V[i] = Q(i, Q_P);
 
         // ------------------------------------------------------------ time steps
-        for (int step = 1; run && step < sh.t_dim; ++step) {
+        for (int step = 1; run && step < T; ++step) {
             double y[M];
             // interior: z = T_I^-1 V_I (forward with l, backward with u and 1/d)
             {
@@ -212,7 +213,7 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64_pcr(const PdeBatch b, Fd1d
             }
         }
         // ------------------------------------------------------------ result
-        double* out = vout + (size_t)pde * N;
+        double* out = vout + shape_row(sh, pde);
 #pragma unroll
         for (int i = 0; i < M; ++i)
             if (j0 + i < N) out[j0 + i] = V[i];
@@ -223,15 +224,30 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64_pcr(const PdeBatch b, Fd1d
 namespace {
 
 template <int M>
+int& per_sm_pcr64()
+{
+    static int v = 1;
+    return v;
+}
+
+template <int M>
+void prepare_pcr64()
+{
+    const size_t smem = (size_t)M * kP64Fields * 32 * sizeof(double);
+    cudaFuncSetAttribute(fd1d_solve_fp64_pcr<M, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(fd1d_solve_fp64_pcr<M, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fd1d_solve_fp64_pcr<M, true>, 32, smem);
+    per_sm_pcr64<M>() = per_sm < 1 ? 1 : per_sm;
+}
+
+template <int M>
 int launch_pcr64(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* vout, int32_t* pde_status,
                  int* counters, double* prices, int32_t* status, int sms, cudaStream_t stream, const SolveEvents* ev)
 {
     const size_t smem = (size_t)M * kP64Fields * 32 * sizeof(double);
     auto kern = sh.c == 1. ? fd1d_solve_fp64_pcr<M, true> : fd1d_solve_fp64_pcr<M, false>;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32, smem);
-    if (per_sm < 1) per_sm = 1;
+    const int per_sm = per_sm_pcr64<M>();
     const int blocks = b.m < sms * per_sm ? b.m : sms * per_sm;
     cudaMemsetAsync(counters, 0, 4 * sizeof(int), stream);
     if (ev) cudaEventRecord(ev->start, stream);
@@ -246,6 +262,15 @@ int launch_pcr64(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, do
 }
 
 }  // namespace
+
+void fd1d_pcr64_prepare(int)
+{
+    prepare_pcr64<2>();
+    prepare_pcr64<4>();
+    prepare_pcr64<8>();
+    prepare_pcr64<16>();
+    prepare_pcr64<32>();
+}
 
 int fd1d_pcr64_nodes_per_lane(int x_dim)
 {

@@ -22,125 +22,12 @@
 
 #include "fd1d_kernels.h"
 #include "kwg.h"
-
-struct kwg_ctx {
-    int device = 0;
-    int sms = 0;
-    cudaStream_t stream = nullptr;
-    std::string err;
-    int launches = 0;
-
-    // grow-only device buffers
-    void* d_work = nullptr;  // coefficients + state
-    size_t work_bytes = 0;
-    void* d_io = nullptr;  // packed inputs / outputs
-    size_t io_bytes = 0;
-    int* d_counter = nullptr;  // [0] tile queue, [1] device-timeout flag, [2..3] 64-bit byte count
-    // pinned host staging
-    void* h_io = nullptr;
-    size_t h_io_bytes = 0;
-    // solve-kernel timing (kwg_set_profiling)
-    // autotuner decisions: shape key -> solver (KWG_SOLVER_THOMAS or KWG_SOLVER_PCR)
-    std::map<uint64_t, int> tuned;
-    bool profiling = false;
-    std::vector<kwg::SolveEvents> events;  // pool, reused across reads
-    size_t events_used = 0;
-
-    const kwg::SolveEvents* next_events()
-    {
-        if (!profiling) return nullptr;
-        if (events_used == events.size()) {
-            kwg::SolveEvents e;
-            if (cudaEventCreate(&e.start) != cudaSuccess || cudaEventCreate(&e.stop) != cudaSuccess ||
-                cudaMallocHost(&e.bytes, sizeof(unsigned long long)) != cudaSuccess)
-                return nullptr;
-            events.push_back(e);
-        }
-        *events[events_used].bytes = 0;
-        return &events[events_used++];
-    }
-};
+#include "kwg_ctx.h"
 
 namespace {
 
-size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+using namespace kwgi;
 
-int set_err(kwg_ctx* ctx, int code, const std::string& msg)
-{
-    if (ctx) ctx->err = msg;
-    return code;
-}
-
-int cuda_err(kwg_ctx* ctx, cudaError_t e, const char* what)
-{
-    return set_err(ctx, KWG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
-}
-
-#define KWG_CUDA(ctx, call)                                   \
-    do {                                                      \
-        cudaError_t e_ = (call);                              \
-        if (e_ != cudaSuccess) return cuda_err(ctx, e_, #call); \
-    } while (0)
-
-int ensure_device(kwg_ctx* ctx, void** buf, size_t* cap, size_t need)
-{
-    if (need <= *cap) return KWG_OK;
-    if (*buf) cudaFree(*buf);
-    *buf = nullptr;
-    *cap = 0;
-    cudaError_t e = cudaMalloc(buf, need);
-    if (e != cudaSuccess) return cuda_err(ctx, e, "cudaMalloc");
-    *cap = need;
-    return KWG_OK;
-}
-
-int ensure_host(kwg_ctx* ctx, void** buf, size_t* cap, size_t need)
-{
-    if (need <= *cap) return KWG_OK;
-    if (*buf) cudaFreeHost(*buf);
-    *buf = nullptr;
-    *cap = 0;
-    cudaError_t e = cudaMallocHost(buf, need);
-    if (e != cudaSuccess) return cuda_err(ctx, e, "cudaMallocHost");
-    *cap = need;
-    return KWG_OK;
-}
-
-int check_params(kwg_ctx* ctx, const kwg_fd1d_params* p)
-{
-    if (!p) return set_err(ctx, KWG_ERR_INVALID, "kwg: null params");
-    if (p->x_dim < 3) return set_err(ctx, KWG_ERR_INVALID, "kwg: x_dim must be >= 3");
-    if (p->t_dim < 2) return set_err(ctx, KWG_ERR_INVALID, "kwg: t_dim must be >= 2");
-    if (!(p->theta > 0.) || !(p->theta <= 1.))
-        return set_err(ctx, KWG_ERR_INVALID, "kwg: theta must be in (0, 1]");
-    if (!(p->scale > 0.) || !std::isfinite(p->scale))
-        return set_err(ctx, KWG_ERR_INVALID, "kwg: scale must be positive and finite");
-    if (!(p->density > 0.)) return set_err(ctx, KWG_ERR_INVALID, "kwg: density must be positive");
-    if (p->precision != KWG_FP64 && p->precision != KWG_FP32)
-        return set_err(ctx, KWG_ERR_INVALID, "kwg: unknown precision");
-    if (p->solver < KWG_SOLVER_AUTO || p->solver > KWG_SOLVER_PCR)
-        return set_err(ctx, KWG_ERR_INVALID, "kwg: unknown solver");
-    if (p->precision == KWG_FP64 && p->solver == KWG_SOLVER_PCR && kwg::fd1d_pcr64_nodes_per_lane(p->x_dim) < 0)
-        return set_err(ctx, KWG_ERR_INVALID, "kwg: the FP64 PCR solver supports x_dim <= 1024");
-    if (p->precision == KWG_FP32 && p->solver == KWG_SOLVER_THOMAS)
-        return set_err(ctx, KWG_ERR_INVALID, "kwg: FP32 uses the on-chip partitioned solver (KWG_SOLVER_PCR or AUTO)");
-    if (p->precision == KWG_FP32 && kwg::fd1d_fp32_nodes_per_lane(p->x_dim) < 0)
-        return set_err(ctx, KWG_ERR_INVALID, "kwg: FP32 stepping supports x_dim <= 2048");
-    return KWG_OK;
-}
-
-kwg::Fd1dShape make_shape(const kwg_fd1d_params* p)
-{
-    kwg::Fd1dShape sh;
-    sh.x_dim = p->x_dim;
-    sh.t_dim = p->t_dim;
-    sh.theta = p->theta;
-    sh.c = (1. - p->theta) / p->theta;
-    sh.scale = p->scale;
-    sh.uniform = std::isinf(p->density);
-    sh.density = sh.uniform ? 1. : p->density;
-    return sh;
-}
 
 // Device pointers into one packed buffer holding a batch's inputs and outputs.
 struct IoLayout {
@@ -291,6 +178,7 @@ kwg_ctx* kwg_create(int device)
     kwg_ctx* ctx = new kwg_ctx();
     ctx->device = device;
     cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
+    kwg::fd1d_prepare_kernels(device);
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&ctx->d_counter, 4 * sizeof(int)) != cudaSuccess) {
         kwg_destroy(ctx);
@@ -308,6 +196,7 @@ void kwg_destroy(kwg_ctx* ctx)
     if (ctx->d_io) cudaFree(ctx->d_io);
     if (ctx->d_counter) cudaFree(ctx->d_counter);
     if (ctx->h_io) cudaFreeHost(ctx->h_io);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     for (auto& e : ctx->events) {
         cudaEventDestroy(e.start);
         cudaEventDestroy(e.stop);

@@ -82,6 +82,8 @@ def lib() -> ctypes.CDLL:
     L.kwg_fd1d_price.restype = i32
     L.kwg_fd1d_price_device.argtypes = [vp, vp, sz, ctypes.POINTER(Fd1dParams), dp, dp, vp]
     L.kwg_fd1d_price_device.restype = i32
+    L.kwg_fd1d_price_uneven.argtypes = [vp, vp, vp, vp, sz, ctypes.POINTER(Fd1dParams), dp, dp]
+    L.kwg_fd1d_price_uneven.restype = i32
     L.kwg_autotune.argtypes = [vp, ctypes.POINTER(Fd1dParams), sz, ctypes.POINTER(ctypes.c_double),
                                ctypes.POINTER(ctypes.c_double)]
     L.kwg_autotune.restype = i32
@@ -155,6 +157,18 @@ class Context:
         rc = self._L.kwg_fd1d_price(
             self.ptr, opts.ctypes.data, n, ctypes.byref(params), prices.ctypes.data, status.ctypes.data
         )
+        return rc, prices, status
+
+    def fd1d_price_uneven(self, opts: np.ndarray, x_dims, t_dims, params: Fd1dParams):
+        """Per-option grids.  Returns (rc, prices, status)."""
+        opts = np.ascontiguousarray(opts, dtype=OPTION_DTYPE)
+        xd = np.ascontiguousarray(x_dims, dtype=np.int32)
+        td = np.ascontiguousarray(t_dims, dtype=np.int32)
+        n = len(opts)
+        prices = np.empty(n, np.float64)
+        status = np.empty(n, np.int32)
+        rc = self._L.kwg_fd1d_price_uneven(self.ptr, opts.ctypes.data, xd.ctypes.data, td.ctypes.data, n,
+                                           ctypes.byref(params), prices.ctypes.data, status.ctypes.data)
         return rc, prices, status
 
     def fd1d_price_device(self, d_opts: int, n: int, params: Fd1dParams, d_prices: int, d_status: int,

@@ -21,6 +21,17 @@ REF_SO = os.path.join(_HERE, "_ref", "libkwref.so")
 
 OK, OUT_OF_GRID, SOLVER_ERROR, BAD_INPUT = 0, 1, 2, 3
 
+# kw::Option layout (src/Core/kwAsset.h:12-22): 6 f64, u8, i8, padded to 56 bytes.
+# numpy operations such as concatenate drop the padding, so every entry point
+# converts its input to this exact layout before handing the buffer to C.
+OPTION_DTYPE = np.dtype({"names": ["t", "k", "z", "r", "q", "s", "e", "w"],
+                         "formats": ["<f8", "<f8", "<f8", "<f8", "<f8", "<f8", "u1", "i1"],
+                         "offsets": [0, 8, 16, 24, 32, 40, 48, 49], "itemsize": 56})
+
+
+def _as_options(opts):
+    return np.ascontiguousarray(np.asarray(opts).astype(OPTION_DTYPE, copy=False))
+
 
 class OracleParams(ctypes.Structure):
     _fields_ = [
@@ -91,7 +102,7 @@ def fd1d_price(opts: np.ndarray, nthreads: int = 0, bs: bool = False, **kw):
     L = oracle_lib()
     p = make_params(**kw)
     n = len(opts)
-    opts = np.ascontiguousarray(opts)
+    opts = _as_options(opts)
     prices = np.zeros(n)
     status = np.zeros(n, np.int32)
     err = ctypes.create_string_buffer(512)
@@ -102,7 +113,7 @@ def fd1d_price(opts: np.ndarray, nthreads: int = 0, bs: bool = False, **kw):
 
 
 def bs_price(opts: np.ndarray) -> np.ndarray:
-    opts = np.ascontiguousarray(opts)
+    opts = _as_options(opts)
     out = np.zeros(len(opts))
     oracle_lib().kwor_bs_price(opts.ctypes.data, len(opts), out.ctypes.data)
     return out
@@ -113,7 +124,7 @@ def solve_grid(opt: np.ndarray, **kw):
     p = make_params(**kw)
     x = np.zeros(p.x_dim)
     v = np.zeros(p.x_dim)
-    one = np.ascontiguousarray(opt.reshape(1))
+    one = _as_options(np.asarray(opt).reshape(1))
     rc = oracle_lib().kwor_fd1d_solve_grid(one.ctypes.data, ctypes.byref(p), x.ctypes.data, v.ctypes.data)
     return rc, x, v
 
@@ -123,7 +134,7 @@ def ref_price(opts: np.ndarray, pricer: str = "FD1D", density=-1.0, scale=-1.0, 
     arguments leave the key unset (reference default)."""
     L = ref_lib()
     n = len(opts)
-    opts = np.ascontiguousarray(opts)
+    opts = _as_options(opts)
     prices = np.full(n, np.nan)
     err = ctypes.create_string_buffer(1024)
     secs = ctypes.c_double(0)

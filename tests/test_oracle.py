@@ -123,3 +123,14 @@ def test_reference_matches_oracle_live(kwor):
     assert rc == 0, msg
     rc, msg, got, _ = kwor.fd1d_price(o, t_dim=200, x_dim=300, scale=5.0, density=0.25)
     assert np.array_equal(got, want)
+
+
+def test_option_layout_is_coerced(kwor):
+    """numpy drops the kw::Option padding on concatenate (56 -> 50 bytes); the
+    wrappers convert to the C layout instead of reading a misaligned buffer."""
+    o = golden("edge.npz")["opts"]
+    cat = np.concatenate([o[:3], o[:3]])
+    assert cat.dtype.itemsize != o.dtype.itemsize
+    _, _, a, _ = kwor.fd1d_price(o[:3])
+    _, _, b, _ = kwor.fd1d_price(cat)
+    assert np.array_equal(b, np.concatenate([a, a]))
