@@ -345,6 +345,43 @@ def run_ours(args):
         raise RuntimeError("FP32: options failed")
     err32 = np.abs(p32 - gpu_prices)
 
+    # ---------------------------------------------------------------- uneven batch (config-3 shapes)
+    uneven = {}
+    if not args.no_uneven:
+        o3, xd3, td3 = portfolio.config3(131072, seed=42, start=rank * 131072)
+        ns3 = int((xd3.astype(np.int64) * (td3.astype(np.int64) - 1)).sum())
+        for name, prec in (("fp64", kwg.FP64), ("fp32", kwg.FP32)):
+            p3 = kwg.params(scale=SCALE, density=DENSITY, precision=prec)
+            for _ in range(max(1, args.warmup)):
+                rc, pr3, st3 = ctx.fd1d_price_uneven(o3, xd3, td3, p3)  # first call captures the graph
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                rc, pr3, st3 = ctx.fd1d_price_uneven(o3, xd3, td3, p3)
+                if rc != 0:
+                    raise RuntimeError(ctx.last_error())
+            dt3 = max_over_ranks(time.perf_counter() - t0) / args.steps
+            ctx.set_profiling(True)
+            ctx.fd1d_price_uneven(o3, xd3, td3, p3)
+            sms, sn = ctx.profile_read()
+            ctx.set_profiling(False)
+            uneven[name] = {"options_per_sec_e2e": ws * len(o3) / dt3, "ms_per_batch_e2e": dt3 * 1e3,
+                            "solve_ms": sms, "solve_launches": sn, "node_steps": ns3,
+                            "out_of_grid": int((st3 == kwg.STATUS_OUT_OF_GRID).sum()),
+                            "failed_other": int(((st3 != 0) & (st3 != kwg.STATUS_OUT_OF_GRID)).sum())}
+            if name == "fp64":
+                ref64 = pr3.copy()
+            else:
+                ok = st3 == 0
+                e = np.abs(pr3[ok] - ref64[ok])
+                uneven[name]["max_abs_err_vs_fd64"] = float(e.max())
+                uneven[name]["p99_abs_err_vs_fd64"] = float(np.percentile(e, 99))
+
+    # ---------------------------------------------------------------- autotuner on this shape
+    t_ms, p_ms = ctx.autotune(prm, N_OPTIONS)
+    tuned = {"thomas_solve_ms": t_ms, "pcr_solve_ms": p_ms, "pick": "thomas" if (p_ms < 0 or t_ms <= p_ms)
+             else "pcr"}
+
     if ws > 1:
         torch.distributed.destroy_process_group()
     if rank != 0:
@@ -402,7 +439,11 @@ def run_ours(args):
                               "speedup_vs_fd64": value32 / value,
                               "max_abs_err_vs_fd64": float(err32.max()),
                               "p99_abs_err_vs_fd64": float(np.percentile(err32, 99)),
-                              "gpu_launches_per_step": launches32}},
+                              "gpu_launches_per_step": launches32},
+                     "uneven_config3": dict(uneven, workload="131072 options, per-option x_dim in "
+                                            "{128..2048} by vol*sqrt(T), t_dim=clamp(ceil(512 sqrt(T)),64,2048), "
+                                            "uniform grids, scale 5; kwg_fd1d_price_uneven (host API, CUDA graph)"),
+                     "autotune_config2_shape": tuned},
     }
     print(json.dumps(line), flush=True)
 
@@ -415,6 +456,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--ref-options", type=int, default=256, help="options per reference step")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch (config 3) variant")
     ap.add_argument("--options", type=int, default=N_OPTIONS,
                     help="options per batch (default 32768; smaller values are for profiling captures)")
     ap.add_argument("--t-dim", type=int, default=T_DIM,
