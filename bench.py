@@ -235,6 +235,73 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+SURROGATE_OPTIONS = 1_000_000
+SURROGATE_WEIGHTS = os.path.join(ROOT, "kwinto-cuda_gb300", "surrogate_weights.npz")
+SURROGATE_AUDIT = 0.01
+SURROGATE_CHECK = 32768  # options of the batch re-priced with FD64 for the error report
+
+
+def surrogate_variant(args, ctx, rank, ws, fd32_rate, barrier, max_over_ranks):
+    """Config 5: fresh options through kwg_surrogate_price (host arrays in and out: the
+    network inside its training box, FD32 at 1024 x 1024 for out-of-box options and a
+    1% seeded audit).  Error vs FD64 (1024 x 1024) on a seeded subsample of the batch."""
+    import torch
+
+    import kwg
+    import portfolio
+
+    if not os.path.exists(SURROGATE_WEIGHTS):
+        return {"unavailable": "surrogate_weights.npz not trained (kwinto-cuda_gb300/train_surrogate.py)"}
+    n = args.surrogate_options
+    net = kwg.Surrogate(torch.cuda.current_device())
+    net.load(SURROGATE_WEIGHTS)
+    meta = json.loads(str(np.load(SURROGATE_WEIGHTS)["meta"])) if "meta" in np.load(SURROGATE_WEIGHTS) else {}
+    opts = portfolio.config1_like(n, seed=5005, start=rank * n)
+    fd = kwg.params(t_dim=T_DIM, x_dim=X_DIM, scale=SCALE, density=DENSITY, precision=kwg.FP32)
+    for i in range(max(1, args.warmup)):
+        prices, route, audit = net.price(ctx, opts, fd, SURROGATE_AUDIT, seed=100 + i)
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        prices, route, audit = net.price(ctx, opts, fd, SURROGATE_AUDIT, seed=1000 + i)
+    dt = max_over_ranks(time.perf_counter() - t0) / args.steps
+    barrier()
+    # network alone, inputs resident (device-timed)
+    d_o = torch.from_numpy(opts.view(np.uint8).copy()).cuda()
+    d_p = torch.empty(n, dtype=torch.float64, device="cuda")
+    net.price_device(d_o.data_ptr(), n, d_p.data_ptr())
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        net.price_device(d_o.data_ptr(), n, d_p.data_ptr())
+    e1.record()
+    torch.cuda.synchronize()
+    net_ms = e0.elapsed_time(e1) / args.steps
+    # error vs FD64 on a seeded subsample (all routes)
+    idx = np.sort(np.random.default_rng(77).choice(n, size=min(SURROGATE_CHECK, n), replace=False))
+    p64 = kwg.params(t_dim=T_DIM, x_dim=X_DIM, scale=SCALE, density=DENSITY, precision=kwg.FP64)
+    rc, ref, st = ctx.fd1d_price(opts[idx], p64)
+    if rc != 0:
+        raise RuntimeError(ctx.last_error())
+    err = np.abs(prices[idx] - ref)
+    net.close()
+    rate = ws * n / dt
+    return {"options_per_sec_e2e": rate, "ms_per_batch_e2e": dt * 1e3, "options": n,
+            "speedup_vs_fd32": rate / fd32_rate, "fd32_options_per_sec": fd32_rate,
+            "network_ms_resident": net_ms, "network_options_per_sec_resident": n / (net_ms / 1e3),
+            "routed_network": int((route == kwg.ROUTE_NETWORK).sum()),
+            "routed_audit": int(audit.audited), "routed_out_of_box": int(audit.out_of_box),
+            "routed_fd_failed": int((route == kwg.ROUTE_FD_FAILED).sum()),
+            "audit_abs_max": audit.audit_abs_max,
+            "audit_abs_mean": audit.audit_abs_sum / max(1, audit.audited),
+            "check_sample": len(idx), "p99_abs_err_vs_fd64": float(np.quantile(err, 0.99)),
+            "max_abs_err_vs_fd64": float(err.max()), "mean_abs_err_vs_fd64": float(err.mean()),
+            "training": meta,
+            "workload": "1M fresh config-2-distribution options (seeded), 1% audit, FD32 fallback at "
+                        "1024x1024; kwg_surrogate_price (host arrays, H2D/D2H inside the timing)"}
+
+
 def run_ours(args):
     import torch
 
@@ -377,6 +444,10 @@ def run_ours(args):
                 uneven[name]["max_abs_err_vs_fd64"] = float(e.max())
                 uneven[name]["p99_abs_err_vs_fd64"] = float(np.percentile(e, 99))
 
+    # ---------------------------------------------------------------- surrogate + FD32 fallback (config 5)
+    surrogate = surrogate_variant(args, ctx, rank, ws, value32, barrier, max_over_ranks) if not args.no_surrogate \
+        else {"skipped": "--no-surrogate"}
+
     # ---------------------------------------------------------------- autotuner on this shape
     t_ms, p_ms = ctx.autotune(prm, N_OPTIONS)
     tuned = {"thomas_solve_ms": t_ms, "pcr_solve_ms": p_ms, "pick": "thomas" if (p_ms < 0 or t_ms <= p_ms)
@@ -443,7 +514,8 @@ def run_ours(args):
                      "uneven_config3": dict(uneven, workload="131072 options, per-option x_dim in "
                                             "{128..2048} by vol*sqrt(T), t_dim=clamp(ceil(512 sqrt(T)),64,2048), "
                                             "uniform grids, scale 5; kwg_fd1d_price_uneven (host API, CUDA graph)"),
-                     "autotune_config2_shape": tuned},
+                     "autotune_config2_shape": tuned,
+                     "surrogate_config5": surrogate},
     }
     print(json.dumps(line), flush=True)
 
@@ -457,6 +529,8 @@ def main():
     ap.add_argument("--ref-options", type=int, default=256, help="options per reference step")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch (config 3) variant")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate (config 5) variant")
+    ap.add_argument("--surrogate-options", type=int, default=SURROGATE_OPTIONS)
     ap.add_argument("--options", type=int, default=N_OPTIONS,
                     help="options per batch (default 32768; smaller values are for profiling captures)")
     ap.add_argument("--t-dim", type=int, default=T_DIM,

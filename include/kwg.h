@@ -147,6 +147,71 @@ int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const int32_t* x
  * No counterpart in the reference, which has one CPU solver. */
 int kwg_autotune(kwg_ctx* ctx, const kwg_fd1d_params* p, size_t m, double* thomas_ms, double* pcr_ms);
 
+/* Tensor-core GEMM used by the MLP surrogate: C[m][n] = sum_k A[m][k] B[n][k] with
+ * A, B row-major BF16 in device memory and C row-major FP32, computed by tcgen05
+ * MMAs with an FP32 accumulator in tensor memory.  k must be a multiple of 64.
+ * Asynchronous on `stream` (a cudaStream_t; NULL = legacy default stream).
+ * No counterpart in the reference. */
+int kwg_gemm_bf16(const void* d_a, const void* d_b, float* d_c, int m, int n, int k, void* stream);
+
+/* ---- learned surrogate ------------------------------------------------------------
+ * No counterpart in the reference (it has no learned component).  An MLP
+ * 5 -> 128 -> 128 -> 128 -> 128 -> 1 with SiLU, BF16 weights and FP32 accumulation on
+ * the tcgen05 tensor cores maps (log K/S, vol sqrt T, r T, q T, put/call), normalised
+ * by a training box, to the early-exercise premium over an analytic base:
+ * (FD American price - base)/K, base = the Barone-Adesi-Whaley quadratic
+ * approximation.  Price = max(intrinsic, base + K * premium).  Trained on FD prices.
+ * Layer inputs enter the tensor cores as BF16 pairs (hi + lo, a 16-bit mantissa:
+ * plain BF16 inputs would move log K/S by ~4e-4 and the price by ~0.02); the
+ * 128 -> 1 output layer is an FP32 dot product with BF16 weights. */
+typedef struct kwg_mlp kwg_mlp;
+
+/* Parameters: 5 weight matrices of 128 x 128 (row-major [out][in]; the first layer
+ * uses inputs 0..4, the output layer row 0) followed by 5 bias vectors of 128. */
+#define KWG_MLP_PARAMS (5 * 128 * 128 + 5 * 128)
+
+typedef struct kwg_audit {
+    int64_t audited;       /* options priced by both the network and FD */
+    int64_t out_of_box;    /* options outside the training box, priced by FD */
+    double audit_abs_max;  /* max |network - FD| over the audited options */
+    double audit_abs_sum;
+} kwg_audit;
+
+kwg_mlp* kwg_mlp_create(int device, uint64_t seed); /* He-uniform initial weights */
+void kwg_mlp_destroy(kwg_mlp* h);
+const char* kwg_mlp_last_error(const kwg_mlp* h);
+/* box_lo/box_hi (5 each, raw feature units) may be NULL to keep the current box. */
+int kwg_mlp_set_params(kwg_mlp* h, const float* params, const double* box_lo, const double* box_hi,
+                       float y_scale);
+int kwg_mlp_get_params(kwg_mlp* h, float* params, double* box_lo, double* box_hi, float* y_scale);
+/* Device features [n][5] (normalised, FP32) -> n outputs (the scaled premium). */
+int kwg_mlp_forward(kwg_mlp* h, const float* d_x, int n, float* d_y);
+/* One forward + backward of the loss mean(e^2) on n rows: e = y - t, except where
+ * d_floor[i] > -1e30 (an early-exercise row, whose price is the intrinsic value):
+ * there e = max(0, y - floor).  d_floor may be NULL (no floors).  Gradients of all
+ * KWG_MLP_PARAMS parameters to d_grad (device), loss to *loss (host). */
+int kwg_mlp_gradients(kwg_mlp* h, const float* d_x, const float* d_t, const float* d_floor, int n, float* d_grad,
+                      double* loss);
+/* Device options -> device features [n][5] (FP32, normalised by the training box),
+ * in-box flags and analytic base prices (any output may be NULL): the Barone-Adesi-
+ * Whaley approximation for American options, Black-Scholes for European ones. */
+int kwg_mlp_featurize(kwg_mlp* h, const kwg_option* d_opts, int n, float* d_x, uint8_t* d_inside, double* d_base);
+/* Trains on device options with their FD prices (device): premium targets scaled to
+ * unit standard deviation, exercise-region floors, Adam with a cosine learning-rate
+ * schedule, shuffled minibatches.  *final_loss = mean loss of the last epoch. */
+int kwg_mlp_train(kwg_mlp* h, const kwg_option* d_opts, const double* d_prices, int n, int epochs, int batch,
+                  float lr, uint64_t seed, double* final_loss);
+/* Network prices of device options (no fallback): max(intrinsic, base + K *
+ * premium) for American options; d_inside (may be NULL) flags options inside the
+ * training box. */
+int kwg_mlp_price_device(kwg_mlp* h, const kwg_option* d_opts, int n, double* d_prices, uint8_t* d_inside);
+/* Surrogate pricing of host options: the network for options inside the training
+ * box, the FD solver (fd's grid and precision) for options outside it and for a
+ * seeded random audit fraction, whose network-vs-FD error is reported.  route[i]:
+ * 0 network, 1 audited (FD price returned), 2 out of box (FD), 3 FD failed. */
+int kwg_surrogate_price(kwg_ctx* ctx, kwg_mlp* h, const kwg_option* opts, size_t n, const kwg_fd1d_params* fd,
+                        double audit_frac, uint64_t seed, double* prices, int32_t* route, kwg_audit* audit);
+
 /* Number of kernel launches the last pricing call made (for launch accounting). */
 int kwg_last_launch_count(const kwg_ctx* ctx);
 

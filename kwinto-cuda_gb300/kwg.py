@@ -56,6 +56,21 @@ class Fd1dParams(ctypes.Structure):
     ]
 
 
+class Audit(ctypes.Structure):
+    """struct kwg_audit (include/kwg.h)."""
+
+    _fields_ = [
+        ("audited", ctypes.c_int64),
+        ("out_of_box", ctypes.c_int64),
+        ("audit_abs_max", ctypes.c_double),
+        ("audit_abs_sum", ctypes.c_double),
+    ]
+
+
+MLP_WIDTH, MLP_LAYERS, MLP_IN = 128, 5, 5
+MLP_PARAMS = MLP_LAYERS * MLP_WIDTH * MLP_WIDTH + MLP_LAYERS * MLP_WIDTH
+ROUTE_NETWORK, ROUTE_AUDIT, ROUTE_OUT_OF_BOX, ROUTE_FD_FAILED = 0, 1, 2, 3
+
 _lib = None
 
 
@@ -87,11 +102,32 @@ def lib() -> ctypes.CDLL:
     L.kwg_autotune.argtypes = [vp, ctypes.POINTER(Fd1dParams), sz, ctypes.POINTER(ctypes.c_double),
                                ctypes.POINTER(ctypes.c_double)]
     L.kwg_autotune.restype = i32
+    L.kwg_gemm_bf16.argtypes = [vp, vp, vp, i32, i32, i32, vp]
+    L.kwg_gemm_bf16.restype = i32
     L.kwg_set_profiling.argtypes = [vp, i32]
     L.kwg_set_profiling.restype = i32
     L.kwg_profile_read.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
                                    ctypes.POINTER(ctypes.c_double)]
     L.kwg_profile_read.restype = i32
+    u64, f32, dbl = ctypes.c_uint64, ctypes.c_float, ctypes.c_double
+    L.kwg_mlp_create.argtypes = [i32, u64]
+    L.kwg_mlp_create.restype = vp
+    L.kwg_mlp_destroy.argtypes = [vp]
+    L.kwg_mlp_destroy.restype = None
+    L.kwg_mlp_last_error.argtypes = [vp]
+    L.kwg_mlp_last_error.restype = ctypes.c_char_p
+    L.kwg_mlp_set_params.argtypes = [vp, vp, vp, vp, f32]
+    L.kwg_mlp_get_params.argtypes = [vp, vp, vp, vp, ctypes.POINTER(f32)]
+    L.kwg_mlp_forward.argtypes = [vp, vp, i32, vp]
+    L.kwg_mlp_gradients.argtypes = [vp, vp, vp, vp, i32, vp, ctypes.POINTER(dbl)]
+    L.kwg_mlp_featurize.argtypes = [vp, vp, i32, vp, vp, vp]
+    L.kwg_mlp_train.argtypes = [vp, vp, vp, i32, i32, i32, f32, u64, ctypes.POINTER(dbl)]
+    L.kwg_mlp_price_device.argtypes = [vp, vp, i32, vp, vp]
+    L.kwg_surrogate_price.argtypes = [vp, vp, vp, sz, ctypes.POINTER(Fd1dParams), dbl, u64, dp, dp,
+                                      ctypes.POINTER(Audit)]
+    for name in ("set_params", "get_params", "forward", "gradients", "featurize", "train", "price_device"):
+        getattr(L, "kwg_mlp_" + name).restype = i32
+    L.kwg_surrogate_price.restype = i32
     _lib = L
     return L
 
@@ -176,6 +212,94 @@ class Context:
         """Device pointers in and out (e.g. torch tensors' data_ptr()); asynchronous."""
         return self._L.kwg_fd1d_price_device(self.ptr, d_opts, n, ctypes.byref(params), d_prices, d_status,
                                              stream or None)
+
+
+class Surrogate:
+    """Owns a kwg_mlp: the MLP surrogate of the FD1D price (no reference counterpart)."""
+
+    def __init__(self, device: int = 0, seed: int = 1):
+        self._L = lib()
+        self.ptr = self._L.kwg_mlp_create(device, seed)
+        if not self.ptr:
+            raise RuntimeError(f"kwg_mlp_create({device}) failed: no usable CUDA device")
+
+    def close(self):
+        if self.ptr:
+            self._L.kwg_mlp_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def last_error(self) -> str:
+        return self._L.kwg_mlp_last_error(self.ptr).decode()
+
+    def _check(self, rc: int):
+        if rc:
+            raise RuntimeError(f"kwg_mlp error {rc}: {self.last_error()}")
+
+    def get_params(self):
+        """(params float32[MLP_PARAMS], box_lo[5], box_hi[5], y_scale)."""
+        p = np.empty(MLP_PARAMS, np.float32)
+        lo, hi = np.empty(MLP_IN), np.empty(MLP_IN)
+        ys = ctypes.c_float(0)
+        self._check(self._L.kwg_mlp_get_params(self.ptr, p.ctypes.data, lo.ctypes.data, hi.ctypes.data,
+                                               ctypes.byref(ys)))
+        return p, lo, hi, ys.value
+
+    def set_params(self, params, box_lo=None, box_hi=None, y_scale: float = 1.0):
+        p = np.ascontiguousarray(params, np.float32)
+        if p.size != MLP_PARAMS:
+            raise ValueError(f"expected {MLP_PARAMS} parameters, got {p.size}")
+        lo = None if box_lo is None else np.ascontiguousarray(box_lo, np.float64)
+        hi = None if box_hi is None else np.ascontiguousarray(box_hi, np.float64)
+        self._check(self._L.kwg_mlp_set_params(self.ptr, p.ctypes.data, None if lo is None else lo.ctypes.data,
+                                               None if hi is None else hi.ctypes.data, y_scale))
+
+    def save(self, path: str):
+        p, lo, hi, ys = self.get_params()
+        np.savez(path, params=p, box_lo=lo, box_hi=hi, y_scale=np.float32(ys))
+
+    def load(self, path: str):
+        z = np.load(path)
+        self.set_params(z["params"], z["box_lo"], z["box_hi"], float(z["y_scale"]))
+
+    def forward(self, d_x: int, n: int, d_y: int):
+        self._check(self._L.kwg_mlp_forward(self.ptr, d_x, n, d_y))
+
+    def gradients(self, d_x: int, d_t: int, n: int, d_grad: int, d_floor: int = 0) -> float:
+        loss = ctypes.c_double(0)
+        self._check(self._L.kwg_mlp_gradients(self.ptr, d_x, d_t, d_floor or None, n, d_grad, ctypes.byref(loss)))
+        return loss.value
+
+    def featurize(self, d_opts: int, n: int, d_x: int = 0, d_inside: int = 0, d_base: int = 0):
+        """Features [n][5], in-box flags and analytic base prices (BAW) of device options."""
+        self._check(self._L.kwg_mlp_featurize(self.ptr, d_opts, n, d_x or None, d_inside or None, d_base or None))
+
+    def train(self, d_opts: int, d_prices: int, n: int, epochs: int, batch: int, lr: float, seed: int = 1) -> float:
+        loss = ctypes.c_double(0)
+        self._check(self._L.kwg_mlp_train(self.ptr, d_opts, d_prices, n, epochs, batch, lr, seed,
+                                          ctypes.byref(loss)))
+        return loss.value
+
+    def price_device(self, d_opts: int, n: int, d_prices: int, d_inside: int = 0):
+        self._check(self._L.kwg_mlp_price_device(self.ptr, d_opts, n, d_prices, d_inside or None))
+
+    def price(self, ctx: Context, opts: np.ndarray, fd: Fd1dParams, audit_frac: float = 0.01, seed: int = 1):
+        """Host options -> (prices, route, Audit): the network inside its training box,
+        FD outside it and on the seeded audit sample."""
+        opts = np.ascontiguousarray(opts, dtype=OPTION_DTYPE)
+        n = len(opts)
+        prices = np.empty(n, np.float64)
+        route = np.empty(n, np.int32)
+        a = Audit()
+        self._check(self._L.kwg_surrogate_price(ctx.ptr, self.ptr, opts.ctypes.data, n, ctypes.byref(fd),
+                                                audit_frac, seed, prices.ctypes.data, route.ctypes.data,
+                                                ctypes.byref(a)))
+        return prices, route, a
 
 
 # ----------------------------------------------------------------------------- kw::Config
