@@ -412,6 +412,30 @@ def run_ours(args):
         raise RuntimeError("FP32: options failed")
     err32 = np.abs(p32 - gpu_prices)
 
+    # ---------------------------------------------------------------- FD1D-BS control variate (host API)
+    for _ in range(max(1, args.warmup)):
+        rc, pbs, stbs = ctx.fd1d_bs_price(opts, prm)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        rc, pbs, stbs = ctx.fd1d_bs_price(opts, prm)
+        if rc != 0:
+            raise RuntimeError(ctx.last_error())
+    dtbs = max_over_ranks(time.perf_counter() - t0) / args.steps
+    fd1d_bs = {"options_per_sec_e2e": ws * N_OPTIONS / dtbs, "ms_per_batch_e2e": dtbs * 1e3,
+               "pdes_solved": 2 * N_OPTIONS, "launches": ctx.launch_count()}
+    if not args.no_cpu and rank == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import kwor
+
+        idx = np.arange(0, N_OPTIONS, max(1, N_OPTIONS // 32))
+        rcb, msgb, wantbs, _ = kwor.fd1d_price(opts[idx], bs=True, t_dim=T_DIM, x_dim=X_DIM, scale=SCALE,
+                                               density=DENSITY)
+        if rcb != 0:
+            raise RuntimeError(msgb)
+        fd1d_bs["max_rel_err_vs_oracle"] = float(np.max(np.abs(pbs[idx] - wantbs) / np.abs(wantbs)))
+        fd1d_bs["oracle_sample"] = len(idx)
+
     # ---------------------------------------------------------------- uneven batch (config-3 shapes)
     uneven = {}
     if not args.no_uneven:
@@ -514,6 +538,7 @@ def run_ours(args):
                      "uneven_config3": dict(uneven, workload="131072 options, per-option x_dim in "
                                             "{128..2048} by vol*sqrt(T), t_dim=clamp(ceil(512 sqrt(T)),64,2048), "
                                             "uniform grids, scale 5; kwg_fd1d_price_uneven (host API, CUDA graph)"),
+                     "fd1d_bs_config2": fd1d_bs,
                      "autotune_config2_shape": tuned,
                      "surrogate_config5": surrogate},
     }

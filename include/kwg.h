@@ -101,6 +101,15 @@ const char* kwg_last_error(const kwg_ctx* ctx);
 int kwg_fd1d_price(kwg_ctx* ctx, const kwg_option* opts, size_t n, const kwg_fd1d_params* p,
                    double* prices, int32_t* status);
 
+/* FD1D-BS control variate: prices[i] = FD(opts[i]) + BS(e) - FD(e), e = opts[i] with
+ * European exercise, all FD prices on p's grid.  Replaces
+ * kw::Fd1d_BlackScholes_Pricer::price (src/Pricer/kwFd1d_BlackScholes.cpp:15-42) and
+ * its Black-Scholes leg (src/Pricer/kwBlackScholes.cpp:27-49).  The n options and
+ * their European copies are deduplicated together and solved in one batch; the
+ * combination runs on the GPU.  Status, strict mode and n == 0 as kwg_fd1d_price. */
+int kwg_fd1d_bs_price(kwg_ctx* ctx, const kwg_option* opts, size_t n, const kwg_fd1d_params* p,
+                      double* prices, int32_t* status);
+
 /* Same computation with inputs and outputs already in DEVICE memory and no
  * deduplication (every option is solved as its own PDE).  Asynchronous on `stream`
  * (a cudaStream_t; NULL = the context's stream).  For callers that keep portfolios

@@ -81,6 +81,30 @@ __global__ void unpack_options(const kwg_option* __restrict__ o, int n, double* 
     e[i] = a.e;
 }
 
+// FD1D-BS epilogue (src/Pricer/kwFd1d_BlackScholes.cpp:15-42): asset i < n was solved
+// as given (price[i]) and as its European copy (price[n + i]); the result is
+// price[i] + BS(European copy) - price[n + i].  The Black-Scholes price follows
+// src/Pricer/kwBlackScholes.cpp:27-49 term for term, with the normal CDF as
+// 0.5 (1 + erf(x / sqrt 2)) (src/Math/kwMath.cpp).
+__global__ void bs_control_variate(int n, const double* __restrict__ s, const double* __restrict__ k,
+                                   const int32_t* __restrict__ pde, const double* __restrict__ t,
+                                   const double* __restrict__ z, const double* __restrict__ r,
+                                   const double* __restrict__ q, const int8_t* __restrict__ w,
+                                   double* __restrict__ prices, int32_t* __restrict__ status)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int j = pde[i];
+    const double tt = t[j], zz = z[j], rr = r[j], qq = q[j], ww = (double)w[j], ss = s[i], kk = k[i];
+    const double zt = zz * sqrt(tt);
+    const double d1 = 1 / zt * (log(ss / kk) + (rr - qq + 0.5 * zz * zz) * tt);
+    const double d2 = d1 - zt;
+    auto cdf = [](double x) { return 0.5 * (1 + erf(x / 1.41421356237309504880)); };
+    const double bs = ww * (ss * cdf(ww * d1) * exp(-qq * tt) - kk * cdf(ww * d2) * exp(-rr * tt));
+    prices[i] = prices[i] + (bs - prices[n + i]);
+    if (status[i] == KWG_STATUS_OK) status[i] = status[n + i];
+}
+
 uint64_t shape_key(int precision, int x_dim, int t_dim, int m)
 {
     int mb = 0;
@@ -148,6 +172,121 @@ int run_batch(kwg_ctx* ctx, char* io, const IoLayout& L, int m, int n, const kwg
                                                ctx->d_counter, prices, status, blocks, stream, ctx->next_events());
     }
     KWG_CUDA(ctx, cudaGetLastError());
+    return KWG_OK;
+}
+
+// Host-array pricing (kwg_fd1d_price; with `control_variate`, kwg_fd1d_bs_price).
+// The control variate prices 2n assets in one batch -- the n given and their
+// European copies -- so dedup shares every PDE the two sets have in common, then
+// the device epilogue combines them.
+int price_host(kwg_ctx* ctx, const kwg_option* user_opts, size_t n_user, const kwg_fd1d_params* p, double* prices,
+               int32_t* status, bool control_variate)
+{
+    if (!ctx) return KWG_ERR_INVALID;
+    ctx->err.clear();
+    ctx->launches = 0;
+    if (int rc = check_params(ctx, p)) return rc;
+    if (n_user == 0) return KWG_OK;
+    if (!user_opts || !prices) return set_err(ctx, KWG_ERR_INVALID, "kwg: null options or prices");
+    if (n_user > (size_t)INT32_MAX / 4) return set_err(ctx, KWG_ERR_INVALID, "kwg: batch too large");
+    KWG_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::vector<kwg_option> with_euro;
+    const kwg_option* opts = user_opts;
+    size_t n = n_user;
+    if (control_variate) {
+        with_euro.assign(user_opts, user_opts + n_user);
+        with_euro.resize(2 * n_user);
+        for (size_t i = 0; i < n_user; ++i) {
+            with_euro[n_user + i] = user_opts[i];
+            with_euro[n_user + i].e = 0;
+        }
+        opts = with_euro.data();
+        n = 2 * n_user;
+    }
+
+    // 1. dedup (src/Pricer/kwFd1d.cpp:28-65): sort by (t, r, q, z, e, w).
+    auto key = [&](uint32_t i) {
+        const kwg_option& o = opts[i];
+        return std::tie(o.t, o.r, o.q, o.z, o.e, o.w);
+    };
+    std::vector<uint32_t> order(n);
+    std::iota(order.begin(), order.end(), 0u);
+    std::sort(order.begin(), order.end(), [&](uint32_t l, uint32_t r) { return key(l) < key(r); });
+    std::vector<int32_t> asset2pde(n);
+    std::vector<uint32_t> pde2asset;
+    pde2asset.reserve(n);
+    pde2asset.push_back(order[0]);
+    asset2pde[order[0]] = 0;
+    for (size_t i = 1; i < n; ++i) {
+        const uint32_t l = order[i - 1], r = order[i];
+        const bool equal = (key(l) < key(r)) == (key(r) < key(l));
+        if (!equal) pde2asset.push_back(r);
+        asset2pde[r] = (int32_t)(pde2asset.size() - 1);
+    }
+    const size_t m = pde2asset.size();
+    const size_t m_pad = (m + kwg::kTile - 1) / kwg::kTile * kwg::kTile;
+
+    // 2. pack into pinned memory
+    const IoLayout L = io_layout(m, m_pad, n);
+    if (int rc = ensure_host(ctx, &ctx->h_io, &ctx->h_io_bytes, L.total)) return rc;
+    if (int rc = ensure_device(ctx, &ctx->d_io, &ctx->io_bytes, L.total)) return rc;
+    char* h = (char*)ctx->h_io;
+    double *t = (double*)(h + L.t), *z = (double*)(h + L.z), *r = (double*)(h + L.r), *q = (double*)(h + L.q);
+    int8_t* w = (int8_t*)(h + L.w);
+    uint8_t* e = (uint8_t*)(h + L.e);
+    for (size_t j = 0; j < m; ++j) {
+        const kwg_option& o = opts[pde2asset[j]];
+        t[j] = o.t;
+        z[j] = o.z;
+        r[j] = o.r;
+        q[j] = o.q;
+        w[j] = o.w;
+        e[j] = o.e;
+    }
+    double *s = (double*)(h + L.s), *k = (double*)(h + L.k);
+    int32_t* pde = (int32_t*)(h + L.pde);
+    for (size_t i = 0; i < n; ++i) {
+        s[i] = opts[i].s;
+        k[i] = opts[i].k;
+        pde[i] = asset2pde[i];
+    }
+    KWG_CUDA(ctx, cudaMemcpyAsync(ctx->d_io, ctx->h_io, L.in_bytes, cudaMemcpyHostToDevice, ctx->stream));
+
+    // 3. kernels
+    char* dio = (char*)ctx->d_io;
+    if (int rc = run_batch(ctx, dio, L, (int)m, (int)n, p, (double*)(dio + L.prices), (int32_t*)(dio + L.status),
+                           ctx->stream))
+        return rc;
+    if (control_variate) {
+        bs_control_variate<<<(unsigned)((n_user + 255) / 256), 256, 0, ctx->stream>>>(
+            (int)n_user, (const double*)(dio + L.s), (const double*)(dio + L.k), (const int32_t*)(dio + L.pde),
+            (const double*)(dio + L.t), (const double*)(dio + L.z), (const double*)(dio + L.r),
+            (const double*)(dio + L.q), (const int8_t*)(dio + L.w), (double*)(dio + L.prices),
+            (int32_t*)(dio + L.status));
+        ctx->launches += 1;
+    }
+
+    // 4. results
+    KWG_CUDA(ctx, cudaMemcpyAsync(h + L.prices, (char*)ctx->d_io + L.prices, L.out_bytes, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    KWG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const double* hp = (const double*)(h + L.prices);
+    const int32_t* hs = (const int32_t*)(h + L.status);
+    std::memcpy(prices, hp, n_user * sizeof(double));
+    if (status) std::memcpy(status, hs, n_user * sizeof(int32_t));
+    if (p->strict) {
+        for (size_t i = 0; i < n_user; ++i) {
+            if (hs[i] == KWG_STATUS_OK) continue;
+            char msg[256];
+            if (hs[i] == KWG_STATUS_OUT_OF_GRID) {
+                std::snprintf(msg, sizeof msg, "Fd1dGpu_Pricer::price: asset %zu: x=%f not in grid range", i,
+                              std::log(opts[i].s / opts[i].k));
+                return set_err(ctx, KWG_ERR_OUT_OF_GRID, msg);
+            }
+            std::snprintf(msg, sizeof msg, "Fd1dGpu_Pricer::price: asset %zu: status %d", i, (int)hs[i]);
+            return set_err(ctx, hs[i] == KWG_STATUS_SOLVER ? KWG_ERR_SOLVER : KWG_ERR_INVALID, msg);
+        }
+    }
     return KWG_OK;
 }
 
@@ -241,91 +380,13 @@ int kwg_profile_read(kwg_ctx* ctx, double* solve_ms, int* solve_launches, double
 int kwg_fd1d_price(kwg_ctx* ctx, const kwg_option* opts, size_t n, const kwg_fd1d_params* p, double* prices,
                    int32_t* status)
 {
-    if (!ctx) return KWG_ERR_INVALID;
-    ctx->err.clear();
-    ctx->launches = 0;
-    if (int rc = check_params(ctx, p)) return rc;
-    if (n == 0) return KWG_OK;
-    if (!opts || !prices) return set_err(ctx, KWG_ERR_INVALID, "kwg: null options or prices");
-    if (n > (size_t)INT32_MAX / 2) return set_err(ctx, KWG_ERR_INVALID, "kwg: batch too large");
-    KWG_CUDA(ctx, cudaSetDevice(ctx->device));
+    return price_host(ctx, opts, n, p, prices, status, false);
+}
 
-    // 1. dedup (src/Pricer/kwFd1d.cpp:28-65): sort by (t, r, q, z, e, w).
-    auto key = [&](uint32_t i) {
-        const kwg_option& o = opts[i];
-        return std::tie(o.t, o.r, o.q, o.z, o.e, o.w);
-    };
-    std::vector<uint32_t> order(n);
-    std::iota(order.begin(), order.end(), 0u);
-    std::sort(order.begin(), order.end(), [&](uint32_t l, uint32_t r) { return key(l) < key(r); });
-    std::vector<int32_t> asset2pde(n);
-    std::vector<uint32_t> pde2asset;
-    pde2asset.reserve(n);
-    pde2asset.push_back(order[0]);
-    asset2pde[order[0]] = 0;
-    for (size_t i = 1; i < n; ++i) {
-        const uint32_t l = order[i - 1], r = order[i];
-        const bool equal = (key(l) < key(r)) == (key(r) < key(l));
-        if (!equal) pde2asset.push_back(r);
-        asset2pde[r] = (int32_t)(pde2asset.size() - 1);
-    }
-    const size_t m = pde2asset.size();
-    const size_t m_pad = (m + kwg::kTile - 1) / kwg::kTile * kwg::kTile;
-
-    // 2. pack into pinned memory
-    const IoLayout L = io_layout(m, m_pad, n);
-    if (int rc = ensure_host(ctx, &ctx->h_io, &ctx->h_io_bytes, L.total)) return rc;
-    if (int rc = ensure_device(ctx, &ctx->d_io, &ctx->io_bytes, L.total)) return rc;
-    char* h = (char*)ctx->h_io;
-    double *t = (double*)(h + L.t), *z = (double*)(h + L.z), *r = (double*)(h + L.r), *q = (double*)(h + L.q);
-    int8_t* w = (int8_t*)(h + L.w);
-    uint8_t* e = (uint8_t*)(h + L.e);
-    for (size_t j = 0; j < m; ++j) {
-        const kwg_option& o = opts[pde2asset[j]];
-        t[j] = o.t;
-        z[j] = o.z;
-        r[j] = o.r;
-        q[j] = o.q;
-        w[j] = o.w;
-        e[j] = o.e;
-    }
-    double *s = (double*)(h + L.s), *k = (double*)(h + L.k);
-    int32_t* pde = (int32_t*)(h + L.pde);
-    for (size_t i = 0; i < n; ++i) {
-        s[i] = opts[i].s;
-        k[i] = opts[i].k;
-        pde[i] = asset2pde[i];
-    }
-    KWG_CUDA(ctx, cudaMemcpyAsync(ctx->d_io, ctx->h_io, L.in_bytes, cudaMemcpyHostToDevice, ctx->stream));
-
-    // 3. kernels
-    char* dio = (char*)ctx->d_io;
-    if (int rc = run_batch(ctx, dio, L, (int)m, (int)n, p, (double*)(dio + L.prices), (int32_t*)(dio + L.status),
-                           ctx->stream))
-        return rc;
-
-    // 4. results
-    KWG_CUDA(ctx, cudaMemcpyAsync(h + L.prices, (char*)ctx->d_io + L.prices, L.out_bytes, cudaMemcpyDeviceToHost,
-                                  ctx->stream));
-    KWG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    const double* hp = (const double*)(h + L.prices);
-    const int32_t* hs = (const int32_t*)(h + L.status);
-    std::memcpy(prices, hp, n * sizeof(double));
-    if (status) std::memcpy(status, hs, n * sizeof(int32_t));
-    if (p->strict) {
-        for (size_t i = 0; i < n; ++i) {
-            if (hs[i] == KWG_STATUS_OK) continue;
-            char msg[256];
-            if (hs[i] == KWG_STATUS_OUT_OF_GRID) {
-                std::snprintf(msg, sizeof msg, "Fd1dGpu_Pricer::price: asset %zu: x=%f not in grid range", i,
-                              std::log(opts[i].s / opts[i].k));
-                return set_err(ctx, KWG_ERR_OUT_OF_GRID, msg);
-            }
-            std::snprintf(msg, sizeof msg, "Fd1dGpu_Pricer::price: asset %zu: status %d", i, (int)hs[i]);
-            return set_err(ctx, hs[i] == KWG_STATUS_SOLVER ? KWG_ERR_SOLVER : KWG_ERR_INVALID, msg);
-        }
-    }
-    return KWG_OK;
+int kwg_fd1d_bs_price(kwg_ctx* ctx, const kwg_option* opts, size_t n, const kwg_fd1d_params* p, double* prices,
+                      int32_t* status)
+{
+    return price_host(ctx, opts, n, p, prices, status, true);
 }
 
 int kwg_autotune(kwg_ctx* ctx, const kwg_fd1d_params* p, size_t m, double* thomas_ms, double* pcr_ms)

@@ -95,6 +95,8 @@ def lib() -> ctypes.CDLL:
     L.kwg_last_launch_count.restype = i32
     L.kwg_fd1d_price.argtypes = [vp, vp, sz, ctypes.POINTER(Fd1dParams), dp, dp]
     L.kwg_fd1d_price.restype = i32
+    L.kwg_fd1d_bs_price.argtypes = [vp, vp, sz, ctypes.POINTER(Fd1dParams), dp, dp]
+    L.kwg_fd1d_bs_price.restype = i32
     L.kwg_fd1d_price_device.argtypes = [vp, vp, sz, ctypes.POINTER(Fd1dParams), dp, dp, vp]
     L.kwg_fd1d_price_device.restype = i32
     L.kwg_fd1d_price_uneven.argtypes = [vp, vp, vp, vp, sz, ctypes.POINTER(Fd1dParams), dp, dp]
@@ -191,6 +193,17 @@ class Context:
         prices = np.empty(n, np.float64)
         status = np.empty(n, np.int32)
         rc = self._L.kwg_fd1d_price(
+            self.ptr, opts.ctypes.data, n, ctypes.byref(params), prices.ctypes.data, status.ctypes.data
+        )
+        return rc, prices, status
+
+    def fd1d_bs_price(self, opts: np.ndarray, params: Fd1dParams):
+        """FD1D-BS control variate, host arrays.  Returns (rc, prices, status)."""
+        opts = np.ascontiguousarray(opts, dtype=OPTION_DTYPE)
+        n = len(opts)
+        prices = np.empty(n, np.float64)
+        status = np.empty(n, np.int32)
+        rc = self._L.kwg_fd1d_bs_price(
             self.ptr, opts.ctypes.data, n, ctypes.byref(params), prices.ctypes.data, status.ctypes.data
         )
         return rc, prices, status
@@ -418,28 +431,44 @@ class Fd1dGpuPricer(Pricer):
             return f"Fd1dGpu_Pricer::init: {ex}"
         return ""
 
+    _name = "Fd1dGpu_Pricer"
+
+    def _solve(self, arr):
+        return self.ctx.fd1d_price(arr, self.params)
+
     def price(self, assets, prices: list) -> str:
         arr = to_array(assets)
         if len(arr) == 0:
             return ""
         if self.ctx is None:
-            return "Fd1dGpu_Pricer::price: init was not called"
-        rc, out, status = self.ctx.fd1d_price(arr, self.params)
+            return f"{self._name}::price: init was not called"
+        rc, out, status = self._solve(arr)
         self.status = status
         prices[:] = out.tolist()
         if rc != KWG_OK:
-            return "Fd1dGpu_Pricer::price: " + self.ctx.last_error()
+            return f"{self._name}::price: " + self.ctx.last_error()
         return ""
 
     def price_array(self, arr: np.ndarray):
         """Fast path: OPTION_DTYPE array -> (error, prices ndarray, status ndarray)."""
-        rc, out, status = self.ctx.fd1d_price(arr, self.params)
-        return ("" if rc == KWG_OK else "Fd1dGpu_Pricer::price: " + self.ctx.last_error()), out, status
+        rc, out, status = self._solve(arr)
+        return ("" if rc == KWG_OK else f"{self._name}::price: " + self.ctx.last_error()), out, status
+
+
+class Fd1dBsGpuPricer(Fd1dGpuPricer):
+    """Drop-in for kw::Fd1d_BlackScholes_Pricer (src/Pricer/kwFd1d_BlackScholes.cpp:15-42):
+    FD(asset) + BS(European copy) - FD(European copy), same FD1D.* keys."""
+
+    _name = "Fd1dBsGpu_Pricer"
+
+    def _solve(self, arr):
+        return self.ctx.fd1d_bs_price(arr, self.params)
 
 
 class PricerFactory:
-    """kw::PricerFactory (src/Pricer/kwPricerFactory.h:15-41).  "FD1D" and "FD1D-GPU"
-    both create the GPU FD pricer (the drop-in); unknown keys are an error."""
+    """kw::PricerFactory (src/Pricer/kwPricerFactory.h:15-41).  "FD1D" / "FD1D-GPU"
+    create the GPU FD pricer, "FD1D-BS" / "FD1D-BS-GPU" its control-variate form
+    (the drop-ins); unknown keys are an error."""
 
     @staticmethod
     def create(config: Config):
@@ -448,6 +477,8 @@ class PricerFactory:
             return "PricerFactory: Missing PRICER key", None
         if mode in ("FD1D", "FD1D-GPU"):
             pricer = Fd1dGpuPricer()
+        elif mode in ("FD1D-BS", "FD1D-BS-GPU"):
+            pricer = Fd1dBsGpuPricer()
         else:
             return f"PricerFactory: Unknown PRICER = {mode}", None
         err = pricer.init(config)
