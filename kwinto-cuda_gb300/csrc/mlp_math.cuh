@@ -44,88 +44,67 @@ __device__ __forceinline__ double bs_euro(const kwg_option& o)
 // A = w (S_c / qe)(1 - e^{-qT} N(w d1(S_c))) on the continuation side of S_c and the
 // intrinsic value beyond it.  Puts with r <= 0 and calls with q <= 0 are never
 // exercised early (the European price), nor are contracts whose S_c lies beyond e^60 K.
+//
+// Precision: E(S) comes in FP64; S_c and the premium term A (S/S_c)^qe are FP32.
+// The price is stationary in S_c at the root (value matching and smooth pasting),
+// so the FP32 root moves it to second order only, and the premium term is a small
+// part of the price: the FP32 parts change the price by ~1e-7 K.
 struct BawSetup {
-    double w, K, lk, zt, mu, qe, dq, dr;
+    float w, K, lk, zt, mu, qe, dq, dr;
 };
 
 __device__ __forceinline__ float ncdf(float x) { return normcdff(x); }
-__device__ __forceinline__ double ncdf(double x) { return normcdf(x); }
-__device__ __forceinline__ float ex(float x) { return expf(x); }
-__device__ __forceinline__ double ex(double x) { return exp(x); }
 
 // g(u) at S = e^u and dg/du; g > 0 on the exercise side (put: below S_c, call: above).
-template <typename F>
-__device__ __forceinline__ F baw_g(const BawSetup& b, F u, F& slope)
+__device__ __forceinline__ float baw_g(const BawSetup& b, float u, float& slope)
 {
-    const F w = (F)b.w, K = (F)b.K, zt = (F)b.zt, qe = (F)b.qe, dq = (F)b.dq;
-    const F s = ex(u);
-    const F d1 = (u - (F)b.lk + (F)b.mu) / zt, d2 = d1 - zt;
-    const F nd1 = ncdf(w * d1);
-    const F e = w * (s * dq * nd1 - K * (F)b.dr * ncdf(w * d2));
-    const F c = F(1) - dq * nd1;
-    const F pdf = F(0.3989422804014327) * ex(F(-0.5) * d1 * d1);
-    slope = s * (w * c * (F(1) - F(1) / qe) + dq * pdf / (zt * qe));
-    return w * (s - K) - e - w * c * s / qe;
-}
-
-// Newton steps in u safeguarded by the sign bracket [lo, hi] (bisection whenever a
-// step leaves it), at most `iters` evaluations, until a step is below tol.
-template <typename F>
-__device__ F baw_root(const BawSetup& b, F u, F lo, F hi, int iters, F tol)
-{
-    for (int it = 0; it < iters; ++it) {
-        F sl;
-        const F gu = baw_g<F>(b, u, sl);
-        if ((gu > F(0)) == (b.w < 0.)) lo = u; else hi = u;
-        F un = u - gu / sl;
-        if (!(un > lo && un < hi)) un = F(0.5) * (lo + hi);
-        const F du = fabs(un - u);
-        u = un;
-        if (du < tol || hi - lo < tol) break;
-    }
-    return u;
+    const float s = expf(u);
+    const float d1 = (u - b.lk + b.mu) / b.zt, d2 = d1 - b.zt;
+    const float nd1 = ncdf(b.w * d1);
+    const float e = b.w * (s * b.dq * nd1 - b.K * b.dr * ncdf(b.w * d2));
+    const float c = 1.f - b.dq * nd1;
+    const float pdf = 0.3989422804f * expf(-0.5f * d1 * d1);
+    slope = s * (b.w * c * (1.f - 1.f / b.qe) + b.dq * pdf / (b.zt * b.qe));
+    return b.w * (s - b.K) - e - b.w * c * s / b.qe;
 }
 
 __device__ inline double baw_price(const kwg_option& o, double euro)
 {
-    const double S = o.s, K = o.k, T = o.t, z = o.z, r = o.r, q = o.q;
+    const float w = o.w < 0 ? -1.f : 1.f;
+    if (w < 0 ? !(o.r > 0.) : !(o.q > 0.)) return euro;
+    const float T = (float)o.t, z = (float)o.z, r = (float)o.r, q = (float)o.q, S = (float)o.s;
     BawSetup b;
-    b.w = o.w < 0 ? -1. : 1.;
-    if (b.w < 0 ? !(r > 0.) : !(q > 0.)) return euro;
-    const double s2 = z * z;
-    b.K = K;
-    b.lk = log(K);
-    b.zt = z * sqrt(T);
-    b.mu = (r - q + 0.5 * s2) * T;
-    const double nn = 2. * (r - q) / s2;
-    const double mk = r * T < 1e-12 ? 2. / (s2 * T) : 2. * r / (s2 * (-expm1(-r * T)));
-    b.qe = 0.5 * (-(nn - 1.) + b.w * sqrt((nn - 1.) * (nn - 1.) + 4. * mk));
-    b.dq = exp(-q * T);
-    b.dr = exp(-r * T);
-    const double lo = b.w < 0 ? b.lk - 60. : b.lk, hi = b.w < 0 ? b.lk : b.lk + 60.;
-    double sl;
-    if (!(baw_g<double>(b, b.w < 0 ? lo : hi, sl) > 0.)) return euro;
-    // FP32 search from one standard deviation off the strike, then FP64 Newton polish;
-    // a polish step that jumps by more than 1e-3 falls back to the FP64 search
-    const float u32 = baw_root<float>(b, (float)(b.lk + b.w * fmin(b.zt, 30.)), (float)lo, (float)hi, 80, 1e-6f);
-    double u = u32;
-    bool ok = true;
-    for (int it = 0; it < 4; ++it) {
-        const double gu = baw_g<double>(b, u, sl);
-        const double du = gu / sl;
-        if (!(fabs(du) < 1e-3)) {
-            ok = false;
-            break;
-        }
-        u -= du;
-        if (fabs(du) < 1e-14) break;
+    b.w = w;
+    b.K = (float)o.k;
+    b.lk = logf(b.K);
+    const float s2 = z * z;
+    b.zt = z * sqrtf(T);
+    b.mu = (r - q + 0.5f * s2) * T;
+    const float nn = 2.f * (r - q) / s2;
+    const float mk = r * T < 1e-6f ? 2.f / (s2 * T) : 2.f * r / (s2 * (-expm1f(-r * T)));
+    b.qe = 0.5f * (-(nn - 1.f) + w * sqrtf((nn - 1.f) * (nn - 1.f) + 4.f * mk));
+    b.dq = expf(-q * T);
+    b.dr = expf(-r * T);
+    float lo = w < 0 ? b.lk - 60.f : b.lk, hi = w < 0 ? b.lk : b.lk + 60.f;
+    float sl;
+    if (!(baw_g(b, w < 0 ? lo : hi, sl) > 0.f)) return euro;
+    // Newton in u = log S from one standard deviation off the strike, safeguarded by
+    // the sign bracket (bisection whenever a step leaves it)
+    float u = b.lk + w * fminf(b.zt, 30.f);
+    for (int it = 0; it < 60; ++it) {
+        const float gu = baw_g(b, u, sl);
+        if ((gu > 0.f) == (w < 0.f)) lo = u; else hi = u;
+        float un = u - gu / sl;
+        if (!(un > lo && un < hi)) un = 0.5f * (lo + hi);
+        const float du = fabsf(un - u);
+        u = un;
+        if (du < 2e-7f * fmaxf(1.f, fabsf(u)) || hi - lo < 2e-7f * fmaxf(1.f, fabsf(u))) break;
     }
-    if (!ok) u = baw_root<double>(b, b.lk + b.w * fmin(b.zt, 30.), lo, hi, 200, 1e-14);
-    const double sc = exp(u);
-    const double d1c = (u - b.lk + b.mu) / b.zt;
-    const double a = b.w * (sc / b.qe) * (1. - b.dq * normcdf(b.w * d1c));
-    const bool cont = b.w < 0 ? S > sc : S < sc;
-    const double v = cont ? euro + a * exp(b.qe * log(S / sc)) : b.w * (S - K);
+    const float sc = expf(u);
+    const float d1c = (u - b.lk + b.mu) / b.zt;
+    const float a = w * (sc / b.qe) * (1.f - b.dq * ncdf(w * d1c));
+    const bool cont = w < 0 ? S > sc : S < sc;
+    const double v = cont ? euro + (double)(a * expf(b.qe * logf(S / sc))) : (double)w * (o.s - o.k);
     return fmax(v, euro);
 }
 
