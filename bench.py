@@ -472,6 +472,45 @@ def run_ours(args):
     surrogate = surrogate_variant(args, ctx, rank, ws, value32, barrier, max_over_ranks) if not args.no_surrogate \
         else {"skipped": "--no-surrogate"}
 
+    # ---------------------------------------------------------------- precision study (config 4)
+    config4 = {"skipped": "--no-config4"}
+    if not args.no_config4:
+        o4 = portfolio.config1_like(65536, seed=44, start=rank * 65536)
+        res4 = {}
+        for name, prec in (("fp64", kwg.FP64), ("fp32", kwg.FP32)):
+            p4 = kwg.params(t_dim=2048, x_dim=2048, scale=SCALE, density=0.25, precision=prec)
+            rc, pr4, st4 = ctx.fd1d_price(o4, p4)  # warm-up (allocations)
+            barrier()
+            t0 = time.perf_counter()
+            rc, pr4, st4 = ctx.fd1d_price(o4, p4)
+            if rc != 0:
+                raise RuntimeError(ctx.last_error())
+            dt4 = max_over_ranks(time.perf_counter() - t0)
+            res4[name] = (pr4, st4, dt4)
+        p64_, s64_, t64_ = res4["fp64"]
+        p32_, s32_, t32_ = res4["fp32"]
+        ok4 = (s64_ == 0) & (s32_ == 0)
+        e_abs = np.abs(p32_[ok4] - p64_[ok4])
+        e_rel = e_abs / np.maximum(np.abs(p64_[ok4]), 1e-12)
+        config4 = {"options": len(o4), "x_dim": 2048, "t_dim": 2048, "density": 0.25, "scale": SCALE,
+                   "fd64_options_per_sec_e2e": ws * len(o4) / t64_, "fd32_options_per_sec_e2e": ws * len(o4) / t32_,
+                   "fd32_speedup": t64_ / t32_,
+                   "fd32_max_abs_err_vs_fd64": float(e_abs.max()),
+                   "fd32_p99_abs_err_vs_fd64": float(np.percentile(e_abs, 99)),
+                   "fd32_max_rel_err_vs_fd64": float(e_rel.max()),
+                   "fd32_p99_rel_err_vs_fd64": float(np.percentile(e_rel, 99)),
+                   "failed": int((~ok4).sum())}
+        if not args.no_cpu and rank == 0:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import kwor
+
+            idx = np.linspace(0, len(o4) - 1, 16).astype(int)
+            rc4, msg4, want4, _ = kwor.fd1d_price(o4[idx], t_dim=2048, x_dim=2048, scale=SCALE, density=0.25)
+            if rc4 != 0:
+                raise RuntimeError(msg4)
+            config4["fd64_max_rel_err_vs_oracle"] = float(np.max(np.abs(p64_[idx] - want4) / np.abs(want4)))
+            config4["oracle_sample"] = len(idx)
+
     # ---------------------------------------------------------------- autotuner on this shape
     t_ms, p_ms = ctx.autotune(prm, N_OPTIONS)
     tuned = {"thomas_solve_ms": t_ms, "pcr_solve_ms": p_ms, "pick": "thomas" if (p_ms < 0 or t_ms <= p_ms)
@@ -539,6 +578,7 @@ def run_ours(args):
                                             "{128..2048} by vol*sqrt(T), t_dim=clamp(ceil(512 sqrt(T)),64,2048), "
                                             "uniform grids, scale 5; kwg_fd1d_price_uneven (host API, CUDA graph)"),
                      "fd1d_bs_config2": fd1d_bs,
+                     "precision_config4": config4,
                      "autotune_config2_shape": tuned,
                      "surrogate_config5": surrogate},
     }
@@ -555,6 +595,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch (config 3) variant")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate (config 5) variant")
+    ap.add_argument("--no-config4", action="store_true", help="skip the 2048x2048 precision study (config 4)")
     ap.add_argument("--surrogate-options", type=int, default=SURROGATE_OPTIONS)
     ap.add_argument("--options", type=int, default=N_OPTIONS,
                     help="options per batch (default 32768; smaller values are for profiling captures)")
