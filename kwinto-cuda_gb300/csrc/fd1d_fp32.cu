@@ -34,9 +34,12 @@ namespace kwg {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kF32Fields = 11;
-// table fields per node, layout [node-in-lane][field][lane] (conflict-free)
-enum { T_C1 = 0, T_C2, T_C3, T_C4, T_L, T_ID, T_U, T_SL, T_SR, T_PH, T_PL };
+// table fields per node, layout [node-in-lane][field][lane] (conflict-free).  On a
+// uniform grid without padded nodes the residual coefficients c1..c4 are the same
+// at every interior node, so they live in registers and the table keeps 7 fields.
+enum { T_L = 0, T_ID, T_U, T_SL, T_SR, T_PH, T_PL, T_C1, T_C2, T_C3, T_C4 };
+template <bool kUni>
+__host__ __device__ constexpr int f32_fields() { return kUni ? 7 : 11; }
 
 struct FF {
     float hi, lo;
@@ -64,13 +67,14 @@ __device__ __forceinline__ void ff_add(float& h, float& l, float d)
 
 }  // namespace
 
-template <int M>
+template <int M, bool kUni>
 __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShape sh, double* __restrict__ vout,
                                                       int32_t* __restrict__ pde_status, int* __restrict__ counters)
 {
-    extern __shared__ float tab[];  // [M][kF32Fields][32]
+    constexpr int kF = f32_fields<kUni>();
+    extern __shared__ float tab[];  // [M][kF][32]
     const int k = threadIdx.x & 31;
-    auto T = [&](int i, int f) -> float& { return tab[(i * kF32Fields + f) * 32 + k]; };
+    auto T = [&](int i, int f) -> float& { return tab[(i * kF + f) * 32 + k]; };
     const int j0 = k * M;
 
     for (;;) {
@@ -98,6 +102,19 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
         // spike end values the separator system needs (L_1, L_{M-1}, R_1, R_{M-1}).
         // The separator system nearly cancels when theta dt sigma^2/dx^2 is large, so
         // its coefficients come from FP64; the per-step arrays are stored in FP32.
+        // uniform grid: interior residual coefficients and the two boundary ones
+        float c1u = 0.f, c2u = 0.f, c3u = 0.f, c4u = 0.f, c2b = 0.f, c3b = 0.f;
+        if (kUni) {
+            const double x0 = g.x(0), x1 = g.x(1), x2 = g.x(2);
+            const double iu = 1. / (x2 - x1), im = 1. / (x2 - x0), id = 1. / (x1 - x0);
+            const double u2 = 2. * iu * im, l2 = 2. * id * im;
+            c1u = (float)(dt * a.axx * l2);
+            c2u = (float)(dt * (a.axx * (u2 - l2) + a.ax * im));
+            c3u = (float)(dt * a.ax * im);
+            c4u = (float)(dt * a.a0);
+            c2b = (float)(dt * a.ax / (x1 - x0));
+            c3b = (float)(dt * a.ax / (g.x(N - 1) - g.x(N - 2)));
+        }
         double bla = 0., ba = 1., bua = 0.;          // separator row (node kM)
         double L1 = 0., Llast = 0., R1 = 0., Rlast = 0.;
         double bl_first_f = 0., bu_last_f = 0.;   // first interior bl, last interior bu
@@ -133,10 +150,12 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
                     // the payoff is exactly 0 on the out-of-the-money side: skip exp there
                     if ((w < 0) ? (x0 < 0.) : (x0 > 0.)) p = split(payoff(w, x0));
                 }
-                T(i, T_C1) = c1;
-                T(i, T_C2) = c2;
-                T(i, T_C3) = c3;
-                T(i, T_C4) = c4;
+                if (!kUni) {
+                    T(i, T_C1) = c1;
+                    T(i, T_C2) = c2;
+                    T(i, T_C3) = c3;
+                    T(i, T_C4) = c4;
+                }
                 T(i, T_PH) = p.hi;
                 T(i, T_PL) = p.lo;
                 if (i == 0) {
@@ -267,10 +286,22 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
                 const float hr = (i == M - 1) ? Hp : H[i + 1], lr = (i == M - 1) ? Lp : Lo[i + 1];
                 const float hdu = hr - H[i], hdd = H[i] - hl, ldu = lr - Lo[i], ldd = Lo[i] - ll;
                 const float Dup = hdu + ldu, Ddn = hdd + ldd, S = (hdu - hdd) + (ldu - ldd);
-                float r = T(i, T_C4) * (H[i] + Lo[i]);
-                r = fmaf(T(i, T_C1), S, r);
-                r = fmaf(T(i, T_C2), Dup, r);
-                y[i] = fmaf(T(i, T_C3), Ddn, r);
+                if (kUni) {
+                    float r = c4u * (H[i] + Lo[i]);
+                    r = fmaf(c1u, S, r);
+                    r = fmaf(c2u, Dup, r);
+                    y[i] = fmaf(c3u, Ddn, r);
+                } else {
+                    float r = T(i, T_C4) * (H[i] + Lo[i]);
+                    r = fmaf(T(i, T_C1), S, r);
+                    r = fmaf(T(i, T_C2), Dup, r);
+                    y[i] = fmaf(T(i, T_C3), Ddn, r);
+                }
+            }
+            if (kUni) {  // the one-sided boundary rows (no second difference)
+                if (k == 0) y[0] = fmaf(c2b, (H[1] - H[0]) + (Lo[1] - Lo[0]), c4u * (H[0] + Lo[0]));
+                if (k == 31)
+                    y[M - 1] = fmaf(c3b, (H[M - 1] - H[M - 2]) + (Lo[M - 1] - Lo[M - 2]), c4u * (H[M - 1] + Lo[M - 1]));
             }
             // interior: forward and backward Thomas
             {
@@ -362,34 +393,47 @@ __global__ void fd1d_interp_rows(const PdeBatch b, const AssetBatch a, Fd1dShape
 
 namespace {
 
-// Resident blocks per SM of fd1d_solve_fp32<M>, set by fd1d_fp32_prepare.
-template <int M>
+// Resident blocks per SM of fd1d_solve_fp32<M, kUni>, set by fd1d_fp32_prepare.
+template <int M, bool kUni>
 int& per_sm_fp32()
 {
     static int v = 1;
     return v;
 }
 
-template <int M>
-void prepare_m()
+template <int M, bool kUni>
+constexpr size_t fp32_smem()
 {
-    const size_t smem = (size_t)M * kF32Fields * 32 * sizeof(float);
-    cudaFuncSetAttribute(fd1d_solve_fp32<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return (size_t)M * f32_fields<kUni>() * 32 * sizeof(float);
+}
+
+template <int M, bool kUni>
+void prepare_mu()
+{
+    const size_t smem = fp32_smem<M, kUni>();
+    cudaFuncSetAttribute(fd1d_solve_fp32<M, kUni>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fd1d_solve_fp32<M>, 32, smem);
-    per_sm_fp32<M>() = per_sm < 1 ? 1 : per_sm;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fd1d_solve_fp32<M, kUni>, 32, smem);
+    per_sm_fp32<M, kUni>() = per_sm < 1 ? 1 : per_sm;
 }
 
 template <int M>
-int launch_m(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* vout, int32_t* pde_status,
-             int* counters, double* prices, int32_t* status, int sms, cudaStream_t stream, const SolveEvents* ev)
+void prepare_m()
 {
-    const size_t smem = (size_t)M * kF32Fields * 32 * sizeof(float);
-    const int per_sm = per_sm_fp32<M>();
+    prepare_mu<M, false>();
+    prepare_mu<M, true>();
+}
+
+template <int M, bool kUni>
+int launch_mu(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* vout, int32_t* pde_status,
+              int* counters, double* prices, int32_t* status, int sms, cudaStream_t stream, const SolveEvents* ev)
+{
+    const size_t smem = fp32_smem<M, kUni>();
+    const int per_sm = per_sm_fp32<M, kUni>();
     const int blocks = b.m < sms * per_sm ? b.m : sms * per_sm;
     cudaMemsetAsync(counters, 0, 4 * sizeof(int), stream);
     if (ev) cudaEventRecord(ev->start, stream);
-    fd1d_solve_fp32<M><<<blocks, 32, smem, stream>>>(b, sh, vout, pde_status, counters);
+    fd1d_solve_fp32<M, kUni><<<blocks, 32, smem, stream>>>(b, sh, vout, pde_status, counters);
     if (ev) cudaEventRecord(ev->stop, stream);
     int launches = 1;
     if (a.n > 0) {
@@ -397,6 +441,18 @@ int launch_m(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double
         ++launches;
     }
     return launches;
+}
+
+// The 7-field uniform-grid kernel needs a uniform grid and x_dim == 32 M for every
+// PDE (M >= 2 so that the boundary rows sit in different nodes of a lane).
+template <int M>
+int launch_m(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* vout, int32_t* pde_status,
+             int* counters, double* prices, int32_t* status, int sms, cudaStream_t stream, const SolveEvents* ev)
+{
+    const bool full = sh.pde_x ? sh.full_lanes : sh.x_dim == 32 * M;
+    if (sh.uniform && full)
+        return launch_mu<M, true>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    return launch_mu<M, false>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
 }
 
 }  // namespace

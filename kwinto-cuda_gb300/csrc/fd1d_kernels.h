@@ -55,6 +55,9 @@ struct Fd1dShape {
     const TileDesc* tiles = nullptr;
     const long long* row_off = nullptr;
     long long node_lanes = 0;  // Thomas work arrays: sum over tiles of 32 * n
+    // per-PDE shapes only: every PDE of the launch has x_dim == 32 x its nodes per
+    // lane (no padded nodes), which the warp-per-PDE uniform-grid kernels require
+    bool full_lanes = false;
 };
 
 __host__ __device__ inline int shape_x(const Fd1dShape& sh, int pde) { return sh.pde_x ? sh.pde_x[pde] : sh.x_dim; }

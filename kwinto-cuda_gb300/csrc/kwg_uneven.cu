@@ -134,6 +134,7 @@ extern "C" int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const
     std::vector<long long> rows;
     std::vector<std::pair<int, int>> buckets;  // PCR: [begin, end) slot ranges per bucket
     std::vector<int> bucket_x;
+    std::vector<bool> bucket_full;
     long long node_lanes = 0;
     std::vector<uint32_t> by(m);
     std::iota(by.begin(), by.end(), 0u);
@@ -183,12 +184,15 @@ extern "C" int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const
             slot_pde.push_back(pde);
             rows.push_back(off);
             off += xd(pde);
+            const bool full = (int)xd(pde) == kwg::kTile * mlane(pde);
             if (i == 0 || mlane(pde) != mlane(by[i - 1])) {
                 buckets.push_back({(int)i, (int)i + 1});
                 bucket_x.push_back(xd(pde));
+                bucket_full.push_back(full);
             } else {
                 buckets.back().second = (int)i + 1;
                 bucket_x.back() = std::max(bucket_x.back(), (int)xd(pde));
+                bucket_full.back() = bucket_full.back() && full;
             }
         }
         node_lanes = off;  // rows of final values, in doubles
@@ -272,6 +276,7 @@ extern "C" int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const
                 sb.m = sb.m_pad = end - beg;
                 kwg::Fd1dShape ss = sh;
                 ss.x_dim = bucket_x[bi];
+                ss.full_lanes = bucket_full[bi];
                 ss.pde_x += beg;
                 ss.pde_t += beg;
                 ss.row_off += beg;
@@ -306,7 +311,8 @@ extern "C" int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const
         sig = mix(sig, u);
     }
     for (size_t bi = 0; bi < buckets.size(); ++bi)
-        sig = mix(mix(mix(sig, (uint64_t)buckets[bi].first), (uint64_t)buckets[bi].second), (uint64_t)bucket_x[bi]);
+        sig = mix(mix(mix(mix(sig, (uint64_t)buckets[bi].first), (uint64_t)buckets[bi].second), (uint64_t)bucket_x[bi]),
+                  (uint64_t)bucket_full[bi]);
 
     if (ctx->profiling) {
         const int r = enqueue(ctx->stream);
