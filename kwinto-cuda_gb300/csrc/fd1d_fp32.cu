@@ -1,6 +1,7 @@
-// fd1d_fp32.cu -- FP32 stepping with FP64-accurate state: one warp per PDE, the whole
-// PDE on chip (state in registers, coefficient tables in shared memory), a
-// partitioned tridiagonal solve with warp shuffles for the reduced system.
+// fd1d_fp32.cu -- FP32 stepping with FP64-accurate state: one warp per PDE (two for
+// grids of 1025..2048 nodes), the whole PDE on chip (state in registers, coefficient
+// tables in shared memory), a partitioned tridiagonal solve with a cyclic reduction
+// of the separator system (warp shuffles; shared memory across the warps of a PDE).
 //
 // Numerics.  The reference step B V' = E V (src/Math/kwFd1d.cpp:61-132) is taken in
 // delta form,  V' = max(V + d, p)  with  B d = dt A V  (E = B + dt A), so FP32 only
@@ -16,12 +17,12 @@
 // payoff are computed in FP64 (src/Pricer/kwFd1d.cpp:110-139); the final
 // interpolation reads V = hi + lo in FP64.
 //
-// Solve of B d = r (N_p = 32 M nodes, lane k owns nodes kM .. kM+M-1):
+// Solve of B d = r (N_p = 32 W M nodes, lane k owns nodes kM .. kM+M-1):
 //   * node kM is a separator s_k; nodes kM+1 .. kM+M-1 are lane k's interior;
 //   * interior:  d_I = y - s_k L - s_{k+1} R,  y = B_I^-1 r_I  (local Thomas,
 //     factors and the spikes L, R precomputed once per PDE);
-//   * separators: a 32-unknown tridiagonal system, solved by parallel cyclic
-//     reduction over the warp (5 shuffle levels, multipliers precomputed).
+//   * separators: a 32 W-unknown tridiagonal system, solved by parallel cyclic
+//     reduction (5 + log2 W levels, multipliers precomputed).
 // B, dt and the grid do not change between steps, so all factors are computed once.
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -67,20 +68,49 @@ __device__ __forceinline__ void ff_add(float& h, float& l, float d)
 
 }  // namespace
 
-template <int M, bool kUni>
-__global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShape sh, double* __restrict__ vout,
-                                                      int32_t* __restrict__ pde_status, int* __restrict__ counters)
+// Shared-memory bytes of the lane-exchange area of a W-warp PDE group (W > 1).
+template <int W>
+__host__ __device__ constexpr int f32_xchg_bytes()
+{
+    return W == 1 ? 0 : 32 * W * (8 * 4 + 6 * 8) + 16 * 4;
+}
+
+// W warps share one PDE (NL = 32 W lanes, lane K owns nodes KM .. KM+M-1).  W == 1
+// exchanges lane-boundary values with warp shuffles; W > 1 through shared memory
+// (one block barrier per exchange; the separator reduction runs 5 + log2 W levels).
+template <int M, bool kUni, int W>
+__global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1dShape sh, double* __restrict__ vout,
+                                                          int32_t* __restrict__ pde_status, int* __restrict__ counters)
 {
     constexpr int kF = f32_fields<kUni>();
-    extern __shared__ float tab[];  // [M][kF][32]
-    const int k = threadIdx.x & 31;
-    auto T = [&](int i, int f) -> float& { return tab[(i * kF + f) * 32 + k]; };
-    const int j0 = k * M;
+    constexpr int NL = 32 * W;
+    constexpr int kLevels = W == 1 ? 5 : W == 2 ? 6 : 7;
+    static_assert(W == 1 || W == 2 || W == 4, "1, 2 or 4 warps per PDE");
+    extern __shared__ float tab[];  // [M][kF][NL], then the exchange area (W > 1)
+    const int k = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int K = threadIdx.x;  // lane of the PDE group
+    auto T = [&](int i, int f) -> float& { return tab[(i * kF + f) * NL + K]; };
+    const int j0 = K * M;
+    float2* x_last = reinterpret_cast<float2*>(tab + M * kF * NL);  // [NL] (H, Lo) of each lane's last node
+    float2* x_first = x_last + NL;                                  // [NL] of its first node
+    float* x_y = reinterpret_cast<float*>(x_first + NL);            // [NL]
+    float* x_p0 = x_y + NL;                                         // [NL] x 2: reduction buffers
+    float* x_p1 = x_p0 + NL;
+    float* x_s = x_p1 + NL;                                         // [NL]
+    double* x_d = reinterpret_cast<double*>(x_s + NL);              // [3][NL] setup exchange
+    int* x_i = reinterpret_cast<int*>(x_d + 6 * NL);                // [0] PDE, [1..W] status
 
     for (;;) {
         int pde = 0;
-        if (k == 0) pde = atomicAdd(&counters[0], 1);
-        pde = __shfl_sync(kFull, pde, 0);
+        if constexpr (W == 1) {
+            if (k == 0) pde = atomicAdd(&counters[0], 1);
+            pde = __shfl_sync(kFull, pde, 0);
+        } else {
+            if (K == 0) x_i[0] = atomicAdd(&counters[0], 1);
+            __syncthreads();
+            pde = x_i[0];
+            __syncthreads();
+        }
         if (pde >= b.m) break;
         const int N = shape_x(sh, pde);
         const int TL = shape_t(sh, pde);  // time levels of this PDE
@@ -225,33 +255,61 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
             }
         }
         // separator system (FP64) and its cyclic-reduction multipliers (stored FP32)
-        float ka[5], kc[5], ib;
+        float ka[kLevels], kc[kLevels], ib;
         {
-            double Lprev = __shfl_up_sync(kFull, Llast, 1);
-            double Rprev = __shfl_up_sync(kFull, Rlast, 1);
-            if (k == 0) Lprev = Rprev = 0.;
+            double Lprev, Rprev;
+            if constexpr (W == 1) {
+                Lprev = __shfl_up_sync(kFull, Llast, 1);
+                Rprev = __shfl_up_sync(kFull, Rlast, 1);
+            } else {
+                x_d[K] = Llast;
+                x_d[NL + K] = Rlast;
+                __syncthreads();
+                Lprev = K > 0 ? x_d[K - 1] : 0.;
+                Rprev = K > 0 ? x_d[NL + K - 1] : 0.;
+                __syncthreads();
+            }
+            if (K == 0) Lprev = Rprev = 0.;
             double al = -bla * Lprev;
             double be = ba - bla * Rprev - bua * L1;
             double ga = -bua * R1;
 #pragma unroll
-            for (int lv = 0; lv < 5; ++lv) {
+            for (int lv = 0; lv < kLevels; ++lv) {
                 const int sg = 1 << lv;
-                double alm = __shfl_up_sync(kFull, al, sg), bem = __shfl_up_sync(kFull, be, sg),
-                       gam = __shfl_up_sync(kFull, ga, sg);
-                double alp = __shfl_down_sync(kFull, al, sg), bep = __shfl_down_sync(kFull, be, sg),
-                       gap = __shfl_down_sync(kFull, ga, sg);
-                if (k - sg < 0) {
+                double alm, bem, gam, alp, bep, gap;
+                if constexpr (W == 1) {
+                    alm = __shfl_up_sync(kFull, al, sg);
+                    bem = __shfl_up_sync(kFull, be, sg);
+                    gam = __shfl_up_sync(kFull, ga, sg);
+                    alp = __shfl_down_sync(kFull, al, sg);
+                    bep = __shfl_down_sync(kFull, be, sg);
+                    gap = __shfl_down_sync(kFull, ga, sg);
+                } else {
+                    x_d[K] = al;
+                    x_d[NL + K] = be;
+                    x_d[2 * NL + K] = ga;
+                    __syncthreads();
+                    const int im = K - sg >= 0 ? K - sg : K, ip = K + sg < NL ? K + sg : K;
+                    alm = x_d[im];
+                    bem = x_d[NL + im];
+                    gam = x_d[2 * NL + im];
+                    alp = x_d[ip];
+                    bep = x_d[NL + ip];
+                    gap = x_d[2 * NL + ip];
+                    __syncthreads();
+                }
+                if (K - sg < 0) {
                     alm = 0.;
                     bem = 1.;
                     gam = 0.;
                 }
-                if (k + sg > 31) {
+                if (K + sg > NL - 1) {
                     alp = 0.;
                     bep = 1.;
                     gap = 0.;
                 }
-                const double ma = (k - sg < 0) ? 0. : al / bem;
-                const double mc = (k + sg > 31) ? 0. : ga / bep;
+                const double ma = (K - sg < 0) ? 0. : al / bem;
+                const double mc = (K + sg > NL - 1) ? 0. : ga / bep;
                 ka[lv] = (float)ma;
                 kc[lv] = (float)mc;
                 const double nal = -ma * alm, nga = -mc * gap;
@@ -264,6 +322,13 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
         }
         const float blaf = (float)bla, buaf = (float)bua;
         st = __reduce_max_sync(kFull, st);
+        if constexpr (W > 1) {
+            if (k == 0) x_i[1 + warp] = st;
+            __syncthreads();
+#pragma unroll
+            for (int v = 0; v < W; ++v) st = max(st, x_i[1 + v]);
+            __syncthreads();
+        }
         const bool run = st == KWG_STATUS_OK;
         float H[M], Lo[M];  // V as float-float pairs, starting at the payoff
 #pragma unroll
@@ -274,10 +339,24 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
 
         // ------------------------------------------------------------ time steps
         for (int step = 1; run && step < TL; ++step) {
-            float Hm = __shfl_up_sync(kFull, H[M - 1], 1), Lm = __shfl_up_sync(kFull, Lo[M - 1], 1);
-            float Hp = __shfl_down_sync(kFull, H[0], 1), Lp = __shfl_down_sync(kFull, Lo[0], 1);
-            if (k == 0) Hm = Lm = 0.f;
-            if (k == 31) Hp = Lp = 0.f;
+            float Hm, Lm, Hp, Lp;
+            if constexpr (W == 1) {
+                Hm = __shfl_up_sync(kFull, H[M - 1], 1);
+                Lm = __shfl_up_sync(kFull, Lo[M - 1], 1);
+                Hp = __shfl_down_sync(kFull, H[0], 1);
+                Lp = __shfl_down_sync(kFull, Lo[0], 1);
+            } else {
+                x_last[K] = make_float2(H[M - 1], Lo[M - 1]);
+                x_first[K] = make_float2(H[0], Lo[0]);
+                __syncthreads();
+                const float2 pm = x_last[K > 0 ? K - 1 : 0], pp = x_first[K < NL - 1 ? K + 1 : 0];
+                Hm = pm.x;
+                Lm = pm.y;
+                Hp = pp.x;
+                Lp = pp.y;
+            }
+            if (K == 0) Hm = Lm = 0.f;
+            if (K == NL - 1) Hp = Lp = 0.f;
             float y[M];
             // residual r = dt A V from exact float-float differences
 #pragma unroll
@@ -299,8 +378,8 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
                 }
             }
             if (kUni) {  // the one-sided boundary rows (no second difference)
-                if (k == 0) y[0] = fmaf(c2b, (H[1] - H[0]) + (Lo[1] - Lo[0]), c4u * (H[0] + Lo[0]));
-                if (k == 31)
+                if (K == 0) y[0] = fmaf(c2b, (H[1] - H[0]) + (Lo[1] - Lo[0]), c4u * (H[0] + Lo[0]));
+                if (K == NL - 1)
                     y[M - 1] = fmaf(c3b, (H[M - 1] - H[M - 2]) + (Lo[M - 1] - Lo[M - 2]), c4u * (H[M - 1] + Lo[M - 1]));
             }
             // interior: forward and backward Thomas
@@ -315,19 +394,54 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
                 for (int i = M - 2; i >= 1; --i) y[i] = fmaf(-T(i, T_U), y[i + 1], y[i]);
             }
             // separators: right-hand side, cyclic reduction, back to the interior
-            float ylp = __shfl_up_sync(kFull, y[M - 1], 1);
-            if (k == 0) ylp = 0.f;
+            float ylp;
+            if constexpr (W == 1) {
+                ylp = __shfl_up_sync(kFull, y[M - 1], 1);
+            } else {
+                x_y[K] = y[M - 1];
+                __syncthreads();
+                ylp = x_y[K > 0 ? K - 1 : 0];
+            }
+            if (K == 0) ylp = 0.f;
             float rho = y[0] - blaf * ylp - buaf * y[1];
+            if constexpr (W == 1) {
 #pragma unroll
-            for (int lv = 0; lv < 5; ++lv) {
-                const int sg = 1 << lv;
-                const float rm = __shfl_up_sync(kFull, rho, sg);
-                const float rp = __shfl_down_sync(kFull, rho, sg);
-                rho = rho - ka[lv] * rm - kc[lv] * rp;
+                for (int lv = 0; lv < kLevels; ++lv) {
+                    const int sg = 1 << lv;
+                    const float rm = __shfl_up_sync(kFull, rho, sg);
+                    const float rp = __shfl_down_sync(kFull, rho, sg);
+                    rho = rho - ka[lv] * rm - kc[lv] * rp;
+                }
+            } else {
+                float* cur = x_p0;
+                float* nxt = x_p1;
+                cur[K] = rho;
+                __syncthreads();
+#pragma unroll
+                for (int lv = 0; lv < kLevels; ++lv) {
+                    const int sg = 1 << lv;
+                    const float rm = cur[K - sg >= 0 ? K - sg : K];
+                    const float rp = cur[K + sg < NL ? K + sg : K];
+                    rho = rho - ka[lv] * rm - kc[lv] * rp;  // ka, kc are 0 past the ends
+                    if (lv + 1 < kLevels) {
+                        nxt[K] = rho;
+                        __syncthreads();
+                        float* tmp = cur;
+                        cur = nxt;
+                        nxt = tmp;
+                    }
+                }
             }
             const float s = rho * ib;
-            float s1 = __shfl_down_sync(kFull, s, 1);
-            if (k == 31) s1 = 0.f;
+            float s1;
+            if constexpr (W == 1) {
+                s1 = __shfl_down_sync(kFull, s, 1);
+            } else {
+                x_s[K] = s;
+                __syncthreads();
+                s1 = x_s[K < NL - 1 ? K + 1 : K];
+            }
+            if (K == NL - 1) s1 = 0.f;
             y[0] = s;
 #pragma unroll
             for (int i = 1; i < M; ++i) y[i] = fmaf(-s1, T(i, T_SR), fmaf(-s, T(i, T_SL), y[i]));
@@ -349,7 +463,7 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp32(const PdeBatch b, Fd1dShap
 #pragma unroll
         for (int i = 0; i < M; ++i)
             if (j0 + i < N) V[j0 + i] = (double)H[i] + (double)Lo[i];
-        if (k == 0) pde_status[pde] = st;
+        if (K == 0) pde_status[pde] = st;
     }
 }
 
@@ -393,47 +507,47 @@ __global__ void fd1d_interp_rows(const PdeBatch b, const AssetBatch a, Fd1dShape
 
 namespace {
 
-// Resident blocks per SM of fd1d_solve_fp32<M, kUni>, set by fd1d_fp32_prepare.
-template <int M, bool kUni>
+// Resident blocks per SM of fd1d_solve_fp32<M, kUni, W>, set by fd1d_fp32_prepare.
+template <int M, bool kUni, int W>
 int& per_sm_fp32()
 {
     static int v = 1;
     return v;
 }
 
-template <int M, bool kUni>
+template <int M, bool kUni, int W>
 constexpr size_t fp32_smem()
 {
-    return (size_t)M * f32_fields<kUni>() * 32 * sizeof(float);
+    return (size_t)M * f32_fields<kUni>() * 32 * W * sizeof(float) + f32_xchg_bytes<W>();
 }
 
-template <int M, bool kUni>
+template <int M, bool kUni, int W>
 void prepare_mu()
 {
-    const size_t smem = fp32_smem<M, kUni>();
-    cudaFuncSetAttribute(fd1d_solve_fp32<M, kUni>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = fp32_smem<M, kUni, W>();
+    cudaFuncSetAttribute(fd1d_solve_fp32<M, kUni, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fd1d_solve_fp32<M, kUni>, 32, smem);
-    per_sm_fp32<M, kUni>() = per_sm < 1 ? 1 : per_sm;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fd1d_solve_fp32<M, kUni, W>, 32 * W, smem);
+    per_sm_fp32<M, kUni, W>() = per_sm < 1 ? 1 : per_sm;
 }
 
-template <int M>
+template <int M, int W>
 void prepare_m()
 {
-    prepare_mu<M, false>();
-    prepare_mu<M, true>();
+    prepare_mu<M, false, W>();
+    prepare_mu<M, true, W>();
 }
 
-template <int M, bool kUni>
+template <int M, bool kUni, int W>
 int launch_mu(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* vout, int32_t* pde_status,
               int* counters, double* prices, int32_t* status, int sms, cudaStream_t stream, const SolveEvents* ev)
 {
-    const size_t smem = fp32_smem<M, kUni>();
-    const int per_sm = per_sm_fp32<M, kUni>();
+    const size_t smem = fp32_smem<M, kUni, W>();
+    const int per_sm = per_sm_fp32<M, kUni, W>();
     const int blocks = b.m < sms * per_sm ? b.m : sms * per_sm;
     cudaMemsetAsync(counters, 0, 4 * sizeof(int), stream);
     if (ev) cudaEventRecord(ev->start, stream);
-    fd1d_solve_fp32<M, kUni><<<blocks, 32, smem, stream>>>(b, sh, vout, pde_status, counters);
+    fd1d_solve_fp32<M, kUni, W><<<blocks, 32 * W, smem, stream>>>(b, sh, vout, pde_status, counters);
     if (ev) cudaEventRecord(ev->stop, stream);
     int launches = 1;
     if (a.n > 0) {
@@ -443,28 +557,28 @@ int launch_mu(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, doubl
     return launches;
 }
 
-// The 7-field uniform-grid kernel needs a uniform grid and x_dim == 32 M for every
+// The 7-field uniform-grid kernel needs a uniform grid and x_dim == 32 W M for every
 // PDE (M >= 2 so that the boundary rows sit in different nodes of a lane).
-template <int M>
+template <int M, int W>
 int launch_m(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* vout, int32_t* pde_status,
              int* counters, double* prices, int32_t* status, int sms, cudaStream_t stream, const SolveEvents* ev)
 {
-    const bool full = sh.pde_x ? sh.full_lanes : sh.x_dim == 32 * M;
+    const bool full = sh.pde_x ? sh.full_lanes : sh.x_dim == 32 * W * M;
     if (sh.uniform && full)
-        return launch_mu<M, true>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
-    return launch_mu<M, false>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+        return launch_mu<M, true, W>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    return launch_mu<M, false, W>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
 }
 
 }  // namespace
 
 void fd1d_fp32_prepare(int)
 {
-    prepare_m<2>();
-    prepare_m<4>();
-    prepare_m<8>();
-    prepare_m<16>();
-    prepare_m<32>();
-    prepare_m<64>();
+    prepare_m<2, 1>();
+    prepare_m<4, 1>();
+    prepare_m<8, 1>();
+    prepare_m<16, 1>();
+    prepare_m<32, 1>();
+    prepare_m<32, 2>();
 }
 
 int fd1d_fp32_nodes_per_lane(int x_dim)
@@ -482,13 +596,14 @@ int fd1d_fp32_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh
 {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    // grids of up to 1024 nodes: one warp per PDE; 2048: two warps of 32 nodes per lane
     switch (fd1d_fp32_nodes_per_lane(sh.x_dim)) {
-    case 2: return launch_m<2>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
-    case 4: return launch_m<4>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
-    case 8: return launch_m<8>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
-    case 16: return launch_m<16>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
-    case 32: return launch_m<32>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
-    case 64: return launch_m<64>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    case 2: return launch_m<2, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    case 4: return launch_m<4, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    case 8: return launch_m<8, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    case 16: return launch_m<16, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    case 32: return launch_m<32, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    case 64: return launch_m<32, 2>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
     default: return -1;
     }
 }
