@@ -37,8 +37,11 @@
 //     CD [node][3][32]  DOWN coefficients (uh, m, 1/d)
 //     P  [node][32]     payoff
 //     S  [node][32][2]  state (V, h|f), one 16-byte load/store per lane
-// A sweep streams them in stages of kGroup consecutive nodes (one mbarrier, two or
-// three bulk copies per stage); in the middle region the coefficients are not read.
+// A sweep streams them in stages of kGroup consecutive nodes (one mbarrier, one to
+// three bulk copies per stage); in the middle region the coefficients are not read,
+// and where the payoff of every lane of the tile is exactly +0 (the out-of-the-money
+// side of a tile of puts only or calls only; all nodes of European PDEs, which never
+// project) the payoff is not read either: the projection there is max(V, +0).
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -68,6 +71,7 @@ struct Work {
     double* s;
     double* cst;  // [m_pad][6]
     int2* range;  // [m_pad]: first and last node of the middle region (empty: x > y)
+    int2* zero;   // [m_pad]: first and last node of the run where the payoff is +0
 };
 
 __device__ __forceinline__ Work work_of(double* base, int m_pad, long long node_lanes)
@@ -80,6 +84,7 @@ __device__ __forceinline__ Work work_of(double* base, int m_pad, long long node_
     w.s = w.p + nodes;
     w.cst = w.s + nodes * 2;
     w.range = reinterpret_cast<int2*>(w.cst + (size_t)m_pad * kConsts);
+    w.zero = w.range + m_pad;
     return w;
 }
 
@@ -249,6 +254,19 @@ __global__ void __launch_bounds__(128) fd1d_setup_fp64(const PdeBatch b, Fd1dSha
         c[5] = CD(mid, 2);
     }
     wk.range[slot] = make_int2(lo, hi);
+    // payoff-free run: the projection never reads P of a European PDE; an American
+    // put's payoff is +0 on a top run of nodes (x >= 0), a call's on a bottom run
+    int zl = 0, zh = N - 1;
+    if (b.e[src] != 0) {
+        if (w < 0) {
+            zl = N;
+            while (zl > 0 && __double_as_longlong(P(zl - 1)) == 0) --zl;
+        } else {
+            zh = -1;
+            while (zh < N - 1 && __double_as_longlong(P(zh + 1)) == 0) ++zh;
+        }
+    }
+    wk.zero[slot] = make_int2(zl, zh);
     if (slot < b.m) pde_status[slot] = st;
 }
 
@@ -284,26 +302,33 @@ __device__ __forceinline__ void stage_nodes(int g, int N, int& first, int& count
     }
 }
 
-// A stage skips the coefficients when all its nodes lie in the middle region.
+// A stage skips the coefficients when all its nodes lie in the middle region, and
+// the payoff when all its nodes lie in the tile's payoff-free run (same test).
 __device__ __forceinline__ bool stage_compact(int first, int count, int lo, int hi)
 {
     return first >= lo && first + count - 1 <= hi;
 }
 
+// The tile's node ranges: middle region [lo, hi], payoff-free run [zlo, zhi].
+struct Ranges {
+    int lo, hi, zlo, zhi;
+};
+
 // Issues stage visit q covering sweep stage g of this tile.
 template <bool kUp>
-__device__ __forceinline__ void issue(const Ring& r, uint32_t q, const TileView& tv, int g, int N, int lo, int hi)
+__device__ __forceinline__ void issue(const Ring& r, uint32_t q, const TileView& tv, int g, int N, const Ranges& rg)
 {
     int first, count;
     stage_nodes<kUp>(g, N, first, count);
-    const bool compact = stage_compact(first, count, lo, hi);
+    const bool compact = stage_compact(first, count, rg.lo, rg.hi);
+    const bool pfree = stage_compact(first, count, rg.zlo, rg.zhi);
     const int s = (int)(q % kRing);
     unsigned char* st = r.stage + (size_t)s * kStageBytes;
     const uint32_t cb = compact ? 0u : count * kNodeCoefBytes;
-    const uint32_t pb = count * kNodePBytes, sb = count * kNodeSBytes;
+    const uint32_t pb = pfree ? 0u : count * kNodePBytes, sb = count * kNodeSBytes;
     mbar_arrive_expect_tx(&r.bar[s], cb + pb + sb);
     if (!compact) bulk_g2s(st, (kUp ? tv.cu : tv.cd) + (size_t)first * kCoef * kTile, cb, &r.bar[s]);
-    bulk_g2s(st + kStageCoef, tv.p + (size_t)first * kTile, pb, &r.bar[s]);
+    if (!pfree) bulk_g2s(st + kStageCoef, tv.p + (size_t)first * kTile, pb, &r.bar[s]);
     bulk_g2s(st + kStageCoef + kStageP, tv.s + (size_t)first * kTile * 2, sb, &r.bar[s]);
 }
 
@@ -316,8 +341,9 @@ __device__ void drain(const Ring& r, uint32_t from, uint32_t to)
 
 // One sweep over this warp's tile.  Returns false on a wait timeout (already drained).
 template <bool kUp, bool kHalf>
-__device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileView& tv, int lane, int N, int lo,
-                                      int hi, const double* cst, double c, bool amer, bool active, int* err)
+__device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileView& tv, int lane, int N,
+                                      const Ranges& rg, const double* cst, double c, bool amer, bool active,
+                                      int* err)
 {
     const int ng = (N + kGroup - 1) / kGroup;
     const int pre = ng < kRing ? ng : kRing;
@@ -325,7 +351,7 @@ __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileVi
     fence_proxy_async_global();
     __syncwarp();
     if (lane == 0)
-        for (int g = 0; g < pre; ++g) issue<kUp>(ring, q + g, tv, g, N, lo, hi);
+        for (int g = 0; g < pre; ++g) issue<kUp>(ring, q + g, tv, g, N, rg);
     // middle-region constants: UP uses (nh, l, 1/e), DOWN (uh, m, 1/d)
     const double ca = kUp ? cst[0] : cst[3], cb = kUp ? cst[1] : cst[4], cs = kUp ? cst[2] : cst[5];
     double2* sout = reinterpret_cast<double2*>(tv.s) + lane;
@@ -344,7 +370,8 @@ __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileVi
         }
         int first, count;
         stage_nodes<kUp>(g, N, first, count);
-        const bool compact = stage_compact(first, count, lo, hi);
+        const bool compact = stage_compact(first, count, rg.lo, rg.hi);
+        const bool pfree = stage_compact(first, count, rg.zlo, rg.zhi);
         const unsigned char* st = ring.stage + (size_t)s * kStageBytes;
         const double* sc_ = reinterpret_cast<const double*>(st) + lane;
         const double* sp_ = reinterpret_cast<const double*>(st + kStageCoef) + lane;
@@ -354,7 +381,7 @@ __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileVi
         for (int k = 0; k < kGroup; ++k) {
             const int idx = kUp ? k : count - 1 - k;  // processing order within the stage
             if (k < count) {
-                rp[k] = sp_[idx * kTile];
+                rp[k] = pfree ? 0. : sp_[idx * kTile];
                 const double2 sv = ss_[idx * kTile];
                 rv[k] = sv.x;
                 rw[k] = sv.y;
@@ -364,7 +391,7 @@ __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileVi
             }
         }
         __syncwarp();  // stage s fully read before it is refilled
-        if (lane == 0 && g + kRing < ng) issue<kUp>(ring, v + kRing, tv, g + kRing, N, lo, hi);
+        if (lane == 0 && g + kRing < ng) issue<kUp>(ring, v + kRing, tv, g + kRing, N, rg);
 #pragma unroll
         for (int k = 0; k < kGroup; ++k) {
             if (k < count) {
@@ -426,9 +453,13 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64(const PdeBatch b, Fd1dShap
         const int t_lane = shape_t(sh, src);
         const int t_max = sh.tiles ? sh.tiles[tile].t_max : sh.t_dim;
         // the tile's middle region is where every lane's coefficients are frozen
-        const int2 rg = wk.range[slot];
-        const int lo = __reduce_max_sync(0xffffffffu, rg.x);
-        const int hi = __reduce_min_sync(0xffffffffu, rg.y);
+        const int2 mr = wk.range[slot], zr = wk.zero[slot];
+        Ranges rg;
+        rg.lo = __reduce_max_sync(0xffffffffu, mr.x);
+        rg.hi = __reduce_min_sync(0xffffffffu, mr.y);
+        rg.zlo = __reduce_max_sync(0xffffffffu, zr.x);
+        rg.zhi = __reduce_min_sync(0xffffffffu, zr.y);
+        const int lo = rg.lo, hi = rg.hi;
         double cst[kConsts] = {0., 0., 0., 0., 0., 0.};
         if (lo <= hi)
             for (int k = 0; k < kConsts; ++k) cst[k] = wk.cst[(size_t)slot * kConsts + k];
@@ -438,10 +469,12 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64(const PdeBatch b, Fd1dShap
             for (int g = 0; g < ng; ++g) {
                 int first, count;
                 stage_nodes<true>(g, N, first, count);
-                per_up += count * (kNodePBytes + 2 * kNodeSBytes) +
+                per_up += count * 2 * kNodeSBytes +
+                          (stage_compact(first, count, rg.zlo, rg.zhi) ? 0 : count * kNodePBytes) +
                           (stage_compact(first, count, lo, hi) ? 0 : count * kNodeCoefBytes);
                 stage_nodes<false>(g, N, first, count);
-                per_dn += count * (kNodePBytes + 2 * kNodeSBytes) +
+                per_dn += count * 2 * kNodeSBytes +
+                          (stage_compact(first, count, rg.zlo, rg.zhi) ? 0 : count * kNodePBytes) +
                           (stage_compact(first, count, lo, hi) ? 0 : count * kNodeCoefBytes);
             }
             const unsigned long long n_up = (unsigned long long)(t_max / 2);  // passes 1, 3, 5, ...
@@ -450,9 +483,9 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64(const PdeBatch b, Fd1dShap
         }
         for (int pass = 1; pass < t_max; ++pass) {
             const bool act = pass < t_lane;
-            const bool ok = (pass & 1) ? sweep<true, kHalf>(ring, q, tv, lane, N, lo, hi, cst, sh.c, amer, act,
+            const bool ok = (pass & 1) ? sweep<true, kHalf>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act,
                                                             &tile_counter[1])
-                                       : sweep<false, kHalf>(ring, q, tv, lane, N, lo, hi, cst, sh.c, amer, act,
+                                       : sweep<false, kHalf>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act,
                                                              &tile_counter[1]);
             if (!ok) return;
             q += ng;
@@ -533,7 +566,7 @@ void fd1d_prepare_kernels(int device)
 size_t fd1d_fp64_work_bytes_nl(int m_pad, long long node_lanes)
 {
     return (size_t)node_lanes * (2 * kCoef + 1 + 2) * sizeof(double) + (size_t)m_pad * kConsts * sizeof(double) +
-           (size_t)m_pad * sizeof(int2);
+           2 * (size_t)m_pad * sizeof(int2);
 }
 
 size_t fd1d_fp64_work_bytes(int m_pad, int x_dim) { return fd1d_fp64_work_bytes_nl(m_pad, (long long)m_pad * x_dim); }

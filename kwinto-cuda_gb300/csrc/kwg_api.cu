@@ -63,24 +63,6 @@ IoLayout io_layout(size_t m, size_t m_pad, size_t n)
     return L;
 }
 
-// AoS kw::Option layout in device memory -> the SoA arrays of one packed buffer.
-__global__ void unpack_options(const kwg_option* __restrict__ o, int n, double* t, double* z, double* r,
-                               double* q, double* s, double* k, int32_t* pde, int8_t* w, uint8_t* e)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const kwg_option a = o[i];
-    t[i] = a.t;
-    z[i] = a.z;
-    r[i] = a.r;
-    q[i] = a.q;
-    s[i] = a.s;
-    k[i] = a.k;
-    pde[i] = i;
-    w[i] = a.w;
-    e[i] = a.e;
-}
-
 // FD1D-BS epilogue (src/Pricer/kwFd1d_BlackScholes.cpp:15-42): asset i < n was solved
 // as given (price[i]) and as its European copy (price[n + i]); the result is
 // price[i] + BS(European copy) - price[n + i].  The Black-Scholes price follows
@@ -103,6 +85,49 @@ __global__ void bs_control_variate(int n, const double* __restrict__ s, const do
     const double bs = ww * (ss * cdf(ww * d1) * exp(-qq * tt) - kk * cdf(ww * d2) * exp(-rr * tt));
     prices[i] = prices[i] + (bs - prices[n + i]);
     if (status[i] == KWG_STATUS_OK) status[i] = status[n + i];
+}
+
+// Exercise / put-call class of a PDE: European puts, European calls, American puts,
+// American calls.  Tiles of one class let the streaming FP64 kernel skip the payoff
+// where it is zero for every lane (kernels are indifferent to the PDE order).
+__host__ __device__ inline int pde_class(uint8_t e, int8_t w) { return (e ? 2 : 0) + (w < 0 ? 0 : 1); }
+
+// Device path, pass 1: PDEs per class (warp-aggregated atomics).
+__global__ void count_classes(const kwg_option* __restrict__ o, int n, int* __restrict__ counts)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = i < n ? pde_class(o[i].e, o[i].w) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, c);
+    if (c >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&counts[c], __popc(peers));
+}
+
+// Device path, pass 2: AoS options -> the SoA arrays of one packed buffer, each PDE
+// at its class's offset + a slot taken in arrival order; pde[i] points at it.
+__global__ void unpack_options(const kwg_option* __restrict__ o, int n, const int* __restrict__ counts,
+                               int* __restrict__ cursor, double* t, double* z, double* r, double* q, double* s,
+                               double* k, int32_t* pde, int8_t* w, uint8_t* e)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = i < n ? pde_class(o[i].e, o[i].w) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, c);
+    const int leader = __ffs(peers) - 1, lane = threadIdx.x & 31;
+    int base = 0;
+    if (c >= 0 && lane == leader) base = atomicAdd(&cursor[c], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    if (c < 0) return;
+    int off = 0;
+    for (int v = 0; v < c; ++v) off += counts[v];
+    const int slot = off + base + __popc(peers & ((1u << lane) - 1u));
+    const kwg_option a = o[i];
+    t[slot] = a.t;
+    z[slot] = a.z;
+    r[slot] = a.r;
+    q[slot] = a.q;
+    w[slot] = a.w;
+    e[slot] = a.e;
+    s[i] = a.s;
+    k[i] = a.k;
+    pde[i] = slot;
 }
 
 uint64_t shape_key(int precision, int x_dim, int t_dim, int m)
@@ -225,6 +250,22 @@ int price_host(kwg_ctx* ctx, const kwg_option* user_opts, size_t n_user, const k
     }
     const size_t m = pde2asset.size();
     const size_t m_pad = (m + kwg::kTile - 1) / kwg::kTile * kwg::kTile;
+    // PDEs grouped by exercise / put-call class (stable), so tiles are homogeneous
+    {
+        size_t off[5] = {0, 0, 0, 0, 0};
+        for (uint32_t a : pde2asset) ++off[pde_class(opts[a].e, opts[a].w) + 1];
+        for (int c = 0; c < 4; ++c) off[c + 1] += off[c];
+        std::vector<int32_t> moved(m);
+        std::vector<uint32_t> order2(m);
+        for (size_t j = 0; j < m; ++j) {
+            const uint32_t a = pde2asset[j];
+            const size_t to = off[pde_class(opts[a].e, opts[a].w)]++;
+            moved[j] = (int32_t)to;
+            order2[to] = a;
+        }
+        pde2asset.swap(order2);
+        for (size_t i = 0; i < n; ++i) asset2pde[i] = moved[asset2pde[i]];
+    }
 
     // 2. pack into pinned memory
     const IoLayout L = io_layout(m, m_pad, n);
@@ -447,13 +488,17 @@ int kwg_fd1d_price_device(kwg_ctx* ctx, const kwg_option* d_opts, size_t n, cons
     cudaStream_t stream = stream_ ? (cudaStream_t)stream_ : ctx->stream;
     const size_t m = n, m_pad = (m + kwg::kTile - 1) / kwg::kTile * kwg::kTile;
     const IoLayout L = io_layout(m, m_pad, n);
-    if (int rc = ensure_device(ctx, &ctx->d_io, &ctx->io_bytes, L.total)) return rc;
+    if (int rc = ensure_device(ctx, &ctx->d_io, &ctx->io_bytes, L.total + 8 * sizeof(int))) return rc;
     char* io = (char*)ctx->d_io;
-    unpack_options<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(
-        d_opts, (int)n, (double*)(io + L.t), (double*)(io + L.z), (double*)(io + L.r), (double*)(io + L.q),
-        (double*)(io + L.s), (double*)(io + L.k), (int32_t*)(io + L.pde), (int8_t*)(io + L.w),
-        (uint8_t*)(io + L.e));
-    ctx->launches += 1;
+    int* counts = (int*)(io + L.total);  // [4] per-class counts, [4] cursors
+    KWG_CUDA(ctx, cudaMemsetAsync(counts, 0, 8 * sizeof(int), stream));
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    count_classes<<<nb, 256, 0, stream>>>(d_opts, (int)n, counts);
+    unpack_options<<<nb, 256, 0, stream>>>(d_opts, (int)n, counts, counts + 4, (double*)(io + L.t),
+                                           (double*)(io + L.z), (double*)(io + L.r), (double*)(io + L.q),
+                                           (double*)(io + L.s), (double*)(io + L.k), (int32_t*)(io + L.pde),
+                                           (int8_t*)(io + L.w), (uint8_t*)(io + L.e));
+    ctx->launches += 2;
     return run_batch(ctx, io, L, (int)m, (int)n, p, d_prices, d_status, stream);
 }
 
