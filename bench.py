@@ -307,6 +307,7 @@ def run_ours(args):
 
     import kwg
     import portfolio
+    import shard
 
     ws, rank, local = dist_env()
     if ws > 1:
@@ -321,7 +322,7 @@ def run_ours(args):
     stream = torch.cuda.Stream(dev)
 
     # each rank prices its own batch (weak scaling), drawn from its own window of the stream
-    opts = portfolio.config1_like(N_OPTIONS, seed=42, start=rank * N_OPTIONS)
+    opts = shard.config_shard(N_OPTIONS, rank, seed=42)
     prm = kwg.params(t_dim=T_DIM, x_dim=X_DIM, scale=SCALE, density=DENSITY, precision=kwg.FP64)
     d_opts = torch.from_numpy(opts.view(np.uint8).copy()).to(dev)
     d_prices = torch.empty(N_OPTIONS, dtype=torch.float64, device=dev)
@@ -340,11 +341,7 @@ def run_ours(args):
         torch.cuda.synchronize(dev)
 
     def max_over_ranks(x):
-        if ws == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+        return shard.max_over_ranks(x)
 
     # ---------------------------------------------------------------- resident (value)
     for _ in range(args.warmup):
