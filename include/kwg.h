@@ -76,7 +76,10 @@ typedef struct kwg_fd1d_params {
     int32_t strict;    /* 1: return an error for the first bad option, like the
                           reference (src/Pricer/kwFd1d.cpp:154-155); 0 (default):
                           per-option status and NaN, the batch still succeeds */
-    int32_t reserved;
+    int32_t device_dedup; /* kwg_fd1d_price_device only: 1 deduplicates the options on
+                          the device by (t,r,q,z,e,w) like the host path (one stream
+                          synchronisation reads the PDE count); 0 (default) solves every
+                          option as its own PDE, fully asynchronously */
 } kwg_fd1d_params;
 
 typedef struct kwg_ctx kwg_ctx;
@@ -110,11 +113,12 @@ int kwg_fd1d_price(kwg_ctx* ctx, const kwg_option* opts, size_t n, const kwg_fd1
 int kwg_fd1d_bs_price(kwg_ctx* ctx, const kwg_option* opts, size_t n, const kwg_fd1d_params* p,
                       double* prices, int32_t* status);
 
-/* Same computation with inputs and outputs already in DEVICE memory and no
- * deduplication (every option is solved as its own PDE).  Asynchronous on `stream`
- * (a cudaStream_t; NULL = the context's stream).  For callers that keep portfolios
- * resident in HBM.  Replaces kw::Fd1d::solve + kw::Fd1d::value
- * (src/Math/kwFd1d.cpp:11-58, 139-158). */
+/* Same computation with inputs and outputs already in DEVICE memory.  Asynchronous
+ * on `stream` (a cudaStream_t; NULL = the context's stream).  For callers that keep
+ * portfolios resident in HBM.  Without p->device_dedup every option is solved as its
+ * own PDE; with it the options are deduplicated on the device (hash table on the key
+ * of src/Pricer/kwFd1d.cpp:28-65; the call then waits once for the PDE count).
+ * Replaces kw::Fd1d::solve + kw::Fd1d::value (src/Math/kwFd1d.cpp:11-58, 139-158). */
 int kwg_fd1d_price_device(kwg_ctx* ctx, const kwg_option* d_opts, size_t n,
                           const kwg_fd1d_params* p, double* d_prices, int32_t* d_status,
                           void* stream);

@@ -130,6 +130,94 @@ __global__ void unpack_options(const kwg_option* __restrict__ o, int n, const in
     pde[i] = slot;
 }
 
+// ---- device-side dedup (kwg_fd1d_price_device with device_dedup): the key of
+// src/Pricer/kwFd1d.cpp:28-65 in an open-addressing table of 2^k >= 2n slots, each
+// holding 1 + the index of the option that owns a key (0 = empty).  Keys compare by
+// value (+0 == -0; a NaN field never matches, so such options stay separate).
+__device__ __forceinline__ bool same_key(const kwg_option& a, const kwg_option& b)
+{
+    return a.t == b.t && a.r == b.r && a.q == b.q && a.z == b.z && a.e == b.e && a.w == b.w;
+}
+
+__device__ __forceinline__ uint64_t key_hash(const kwg_option& o)
+{
+    uint64_t h = 0x9E3779B97F4A7C15ull;
+    for (double v : {o.t, o.r, o.q, o.z}) {
+        const uint64_t b = v == 0. ? 0ull : (uint64_t)__double_as_longlong(v);
+        h = (h ^ b) * 0xBF58476D1CE4E5B9ull;
+        h ^= h >> 31;
+    }
+    h = (h ^ ((uint64_t)o.e << 8 | (uint8_t)o.w)) * 0x94D049BB133111EBull;
+    return h ^ (h >> 29);
+}
+
+__global__ void dedup_insert(const kwg_option* __restrict__ o, int n, unsigned* __restrict__ table,
+                             unsigned mask, int* __restrict__ owner)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const kwg_option a = o[i];
+    unsigned p = (unsigned)key_hash(a) & mask;
+    int own = i;  // the probe below ends within mask + 1 steps: the table is at most half full
+    for (unsigned it = 0; it <= mask; ++it) {
+        const unsigned cur = atomicCAS(&table[p], 0u, (unsigned)i + 1u);
+        if (cur == 0u) break;
+        if (same_key(o[cur - 1u], a)) {
+            own = (int)(cur - 1u);
+            break;
+        }
+        p = (p + 1u) & mask;
+    }
+    owner[i] = own;
+}
+
+// Owners per class, like count_classes.
+__global__ void dedup_count(const kwg_option* __restrict__ o, int n, const int* __restrict__ owner,
+                            int* __restrict__ counts)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = (i < n && owner[i] == i) ? pde_class(o[i].e, o[i].w) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, c);
+    if (c >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&counts[c], __popc(peers));
+}
+
+// Owners become PDEs at class offset + arrival slot; every option keeps its s, k.
+__global__ void dedup_unpack(const kwg_option* __restrict__ o, int n, const int* __restrict__ owner,
+                             const int* __restrict__ counts, int* __restrict__ cursor, int* __restrict__ slot_of,
+                             double* t, double* z, double* r, double* q, double* s, double* k, int8_t* w,
+                             uint8_t* e)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = (i < n && owner[i] == i) ? pde_class(o[i].e, o[i].w) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, c);
+    const int leader = __ffs(peers) - 1, lane = threadIdx.x & 31;
+    int base = 0;
+    if (c >= 0 && lane == leader) base = atomicAdd(&cursor[c], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    if (i >= n) return;
+    const kwg_option a = o[i];
+    s[i] = a.s;
+    k[i] = a.k;
+    if (c < 0) return;
+    int off = 0;
+    for (int v = 0; v < c; ++v) off += counts[v];
+    const int slot = off + base + __popc(peers & ((1u << lane) - 1u));
+    slot_of[i] = slot;
+    t[slot] = a.t;
+    z[slot] = a.z;
+    r[slot] = a.r;
+    q[slot] = a.q;
+    w[slot] = a.w;
+    e[slot] = a.e;
+}
+
+__global__ void dedup_map(int n, const int* __restrict__ owner, const int* __restrict__ slot_of,
+                          int32_t* __restrict__ pde)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) pde[i] = slot_of[owner[i]];
+}
+
 uint64_t shape_key(int precision, int x_dim, int t_dim, int m)
 {
     int mb = 0;
@@ -331,6 +419,40 @@ int price_host(kwg_ctx* ctx, const kwg_option* user_opts, size_t n_user, const k
     return KWG_OK;
 }
 
+// kwg_fd1d_price_device with device_dedup: the packed buffer is laid out for n PDEs
+// (the upper bound), the dedup kernels fill m <= n of them, and one synchronisation
+// reads m before the solver launches are sized.
+int price_device_dedup(kwg_ctx* ctx, const kwg_option* d_opts, size_t n, size_t n_pad, const kwg_fd1d_params* p,
+                       double* d_prices, int32_t* d_status, cudaStream_t stream)
+{
+    const IoLayout L = io_layout(n, n_pad, n);
+    unsigned cap = 64;
+    while (cap < 2 * n) cap <<= 1;
+    const size_t extra = 8 * sizeof(int) + (size_t)cap * sizeof(unsigned) + 2 * n * sizeof(int);
+    if (int rc = ensure_device(ctx, &ctx->d_io, &ctx->io_bytes, L.total + extra)) return rc;
+    if (int rc = ensure_host(ctx, &ctx->h_io, &ctx->h_io_bytes, 64)) return rc;
+    char* io = (char*)ctx->d_io;
+    int* counts = (int*)(io + L.total);  // [4] per-class counts, [4] cursors
+    unsigned* table = (unsigned*)(counts + 8);
+    int* owner = (int*)(table + cap);
+    int* slot_of = owner + n;
+    KWG_CUDA(ctx, cudaMemsetAsync(counts, 0, 8 * sizeof(int) + (size_t)cap * sizeof(unsigned), stream));
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    dedup_insert<<<nb, 256, 0, stream>>>(d_opts, (int)n, table, cap - 1, owner);
+    dedup_count<<<nb, 256, 0, stream>>>(d_opts, (int)n, owner, counts);
+    dedup_unpack<<<nb, 256, 0, stream>>>(d_opts, (int)n, owner, counts, counts + 4, slot_of, (double*)(io + L.t),
+                                         (double*)(io + L.z), (double*)(io + L.r), (double*)(io + L.q),
+                                         (double*)(io + L.s), (double*)(io + L.k), (int8_t*)(io + L.w),
+                                         (uint8_t*)(io + L.e));
+    dedup_map<<<nb, 256, 0, stream>>>((int)n, owner, slot_of, (int32_t*)(io + L.pde));
+    ctx->launches += 4;
+    int* hc = (int*)ctx->h_io;
+    KWG_CUDA(ctx, cudaMemcpyAsync(hc, counts, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    KWG_CUDA(ctx, cudaStreamSynchronize(stream));
+    const int m = hc[0] + hc[1] + hc[2] + hc[3];
+    return run_batch(ctx, io, L, m, (int)n, p, d_prices, d_status, stream);
+}
+
 }  // namespace
 
 
@@ -347,7 +469,7 @@ void kwg_fd1d_params_default(kwg_fd1d_params* p)
     p->precision = KWG_FP64;
     p->solver = KWG_SOLVER_AUTO;
     p->strict = 0;
-    p->reserved = 0;
+    p->device_dedup = 0;
 }
 
 kwg_ctx* kwg_create(int device)
@@ -486,7 +608,9 @@ int kwg_fd1d_price_device(kwg_ctx* ctx, const kwg_option* d_opts, size_t n, cons
     if (n > (size_t)INT32_MAX / 2) return set_err(ctx, KWG_ERR_INVALID, "kwg: batch too large");
     KWG_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t stream = stream_ ? (cudaStream_t)stream_ : ctx->stream;
-    const size_t m = n, m_pad = (m + kwg::kTile - 1) / kwg::kTile * kwg::kTile;
+    const size_t n_pad = (n + kwg::kTile - 1) / kwg::kTile * kwg::kTile;
+    if (p->device_dedup) return price_device_dedup(ctx, d_opts, n, n_pad, p, d_prices, d_status, stream);
+    const size_t m = n, m_pad = n_pad;
     const IoLayout L = io_layout(m, m_pad, n);
     if (int rc = ensure_device(ctx, &ctx->d_io, &ctx->io_bytes, L.total + 8 * sizeof(int))) return rc;
     char* io = (char*)ctx->d_io;

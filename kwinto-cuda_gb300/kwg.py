@@ -52,7 +52,7 @@ class Fd1dParams(ctypes.Structure):
         ("precision", ctypes.c_int32),
         ("solver", ctypes.c_int32),
         ("strict", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("device_dedup", ctypes.c_int32),
     ]
 
 

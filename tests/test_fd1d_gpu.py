@@ -171,6 +171,36 @@ def test_device_api_matches_host_api(ctx):
     assert (d_s.cpu().numpy() == 0).all()
 
 
+@pytest.mark.parametrize("precision,solver", [(0, 1), (0, 2), (1, 0)], ids=["fp64-thomas", "fp64-pcr", "fp32"])
+def test_device_dedup_matches_host_dedup(ctx, precision, solver):
+    """Device-side dedup (hash table on the key of src/Pricer/kwFd1d.cpp:28-65) on the
+    QuantLib portfolio (6000 puts, 600 distinct keys) plus the edge fixture's
+    duplicates, European options and calls: identical prices and statuses to the
+    host path, which dedups like the reference."""
+    import torch
+
+    import kwg
+
+    o = np.concatenate([golden("portfolio_qdfp.npz")["opts"], golden("edge.npz")["opts"]])
+    o = np.ascontiguousarray(o, dtype=kwg.OPTION_DTYPE)
+    prm = kwg.params(t_dim=256, x_dim=256, scale=50.0, density=0.25, precision=precision, solver=solver)
+    rc, want, want_st = ctx.fd1d_price(o, prm)
+    assert rc == 0, ctx.last_error()
+    prm.device_dedup = 1
+    d_o = torch.from_numpy(o.view(np.uint8).copy()).cuda()
+    d_p = torch.empty(len(o), dtype=torch.float64, device="cuda")
+    d_s = torch.empty(len(o), dtype=torch.int32, device="cuda")
+    rc = ctx.fd1d_price_device(d_o.data_ptr(), len(o), prm, d_p.data_ptr(), d_s.data_ptr(),
+                               torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, ctx.last_error()
+    torch.cuda.synchronize()
+    got = d_p.cpu().numpy()
+    assert np.array_equal(d_s.cpu().numpy(), want_st)
+    ok = want_st == 0
+    assert np.array_equal(got[ok], want[ok])
+    assert np.isnan(got[~ok]).all()
+
+
 def test_pricer_mirror(built):
     """kw::PricerFactory / kw::Pricer usage exactly like test/kwPricer_test.cpp:63-84."""
     import kwg
