@@ -225,6 +225,12 @@ int kwg_mlp_price_device(kwg_mlp* h, const kwg_option* d_opts, int n, double* d_
 int kwg_surrogate_price(kwg_ctx* ctx, kwg_mlp* h, const kwg_option* opts, size_t n, const kwg_fd1d_params* fd,
                         double audit_frac, uint64_t seed, double* prices, int32_t* route, kwg_audit* audit);
 
+/* Self-test of the bounded device waits (no counterpart in the reference): one
+ * kernel waits on an mbarrier that nothing arrives on and must give up after a few
+ * thousand polls (*timed_out = 1), then waits on one it arrived on and must pass
+ * (*completed = 1).  Nothing faults or hangs; the context stays usable. */
+int kwg_selftest_waits(kwg_ctx* ctx, int32_t* timed_out, int32_t* completed);
+
 /* Number of kernel launches the last pricing call made (for launch accounting). */
 int kwg_last_launch_count(const kwg_ctx* ctx);
 

@@ -23,6 +23,7 @@
 #include "fd1d_kernels.h"
 #include "kwg.h"
 #include "kwg_ctx.h"
+#include "tma.cuh"
 
 namespace {
 
@@ -216,6 +217,22 @@ __global__ void dedup_map(int n, const int* __restrict__ owner, const int* __res
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) pde[i] = slot_of[owner[i]];
+}
+
+// Self-test of the bounded waits every kernel uses: out[0] = 1 when a wait on an
+// mbarrier that nothing arrives on gives up after `limit` polls (the timeout path
+// the solvers take before setting their error flags); out[1] = 1 when a wait on an
+// mbarrier this thread arrived on succeeds.  One thread, nothing in flight.
+__global__ void selftest_waits(int32_t* __restrict__ out, uint32_t limit)
+{
+    __shared__ uint64_t bar[2];
+    if (threadIdx.x != 0) return;
+    kwg::mbar_init(&bar[0], 1);
+    kwg::mbar_init(&bar[1], 1);
+    kwg::fence_mbar_init();
+    out[0] = kwg::mbar_wait_n(&bar[0], 0, limit) ? 0 : 1;
+    kwg::mbar_arrive(&bar[1]);
+    out[1] = kwg::mbar_wait_n(&bar[1], 0, limit) ? 1 : 0;
 }
 
 uint64_t shape_key(int precision, int x_dim, int t_dim, int m)
@@ -550,6 +567,24 @@ int kwg_fd1d_bs_price(kwg_ctx* ctx, const kwg_option* opts, size_t n, const kwg_
                       int32_t* status)
 {
     return price_host(ctx, opts, n, p, prices, status, true);
+}
+
+int kwg_selftest_waits(kwg_ctx* ctx, int32_t* timed_out, int32_t* completed)
+{
+    if (!ctx || !timed_out || !completed) return KWG_ERR_INVALID;
+    ctx->err.clear();
+    KWG_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (int rc = ensure_device(ctx, &ctx->d_io, &ctx->io_bytes, 2 * sizeof(int32_t))) return rc;
+    int32_t* d = (int32_t*)ctx->d_io;
+    KWG_CUDA(ctx, cudaMemsetAsync(d, 0xff, 2 * sizeof(int32_t), ctx->stream));
+    selftest_waits<<<1, 32, 0, ctx->stream>>>(d, 4096u);
+    KWG_CUDA(ctx, cudaGetLastError());
+    int32_t h[2] = {-1, -1};
+    KWG_CUDA(ctx, cudaMemcpyAsync(h, d, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+    KWG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *timed_out = h[0];
+    *completed = h[1];
+    return KWG_OK;
 }
 
 int kwg_autotune(kwg_ctx* ctx, const kwg_fd1d_params* p, size_t m, double* thomas_ms, double* pcr_ms)

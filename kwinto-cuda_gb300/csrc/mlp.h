@@ -40,7 +40,12 @@ struct GemmArgs {
 };
 
 size_t gemm_smem_bytes();
+cudaError_t gemm_set_smem_limit();  // on the current device
 cudaError_t gemm_launch(const GemmArgs& g, int splits, cudaStream_t stream);
+
+// Shared-memory limits of the surrogate kernels on the current device, once per
+// device (bit d of a process-wide mask); every launcher calls it first.
+cudaError_t mlp_prepare_device();
 
 // ---- MLP surrogate: 5 -> 128 -> 128 -> 128 -> 128 -> 1, SiLU.
 // Parameters (FP32 master copy): five [128 out][128 in] weight matrices (layer 1 uses

@@ -17,6 +17,7 @@
 // The arithmetic matches the layer-by-layer path (mlp_gemm.cu) step for step.
 // Every MMA completion wait is bounded; on a timeout the kernel sets *error, waits
 // (bounded) for the MMAs in flight and frees its TMEM.
+#include <atomic>
 #include <cstdint>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -197,17 +198,24 @@ __global__ void __launch_bounds__(128, 1)
     if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
+cudaError_t mlp_prepare_device()
+{
+    static std::atomic<unsigned long long> done{0};
+    int dev = 0;
+    if (const cudaError_t e = cudaGetDevice(&dev); e != cudaSuccess) return e;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load() & bit) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(mlp_price_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
+    if (e == cudaSuccess) e = gemm_set_smem_limit();
+    if (e == cudaSuccess) done.fetch_or(bit);
+    return e;
+}
+
 cudaError_t mlp_launch_price_fused(const kwg_option* opts, int n, const MlpBox& box, const __nv_bfloat16* wb,
                                    const float* params, float y_scale, double* prices, uint8_t* inside, int* error,
                                    int sms, cudaStream_t st)
 {
-    static bool attr = false;
-    if (!attr) {
-        const cudaError_t e =
-            cudaFuncSetAttribute(mlp_price_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    if (const cudaError_t e = mlp_prepare_device(); e != cudaSuccess) return e;
     const int tiles = (n + kRows - 1) / kRows;
     const int grid = tiles < sms ? tiles : sms;
     mlp_price_fused<<<grid, kRows, kSmemBytes, st>>>(opts, n, box, wb, params, y_scale, prices, inside, error);

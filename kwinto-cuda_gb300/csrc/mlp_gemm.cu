@@ -148,13 +148,14 @@ __global__ void __launch_bounds__(128) gemm_bf16_tn(const GemmArgs g)
 // memory caps residency at 4 CTAs per SM, so allocations never wait on each other.
 size_t gemm_smem_bytes() { return 56 * 1024; }
 
+cudaError_t gemm_set_smem_limit()
+{
+    return cudaFuncSetAttribute(gemm_bf16_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem_bytes());
+}
+
 cudaError_t gemm_launch(const GemmArgs& g, int splits, cudaStream_t stream)
 {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(gemm_bf16_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem_bytes());
-        attr = true;
-    }
+    if (const cudaError_t e = mlp_prepare_device(); e != cudaSuccess) return e;
     dim3 grid((g.M + kTileM - 1) / kTileM, (g.N + kTileN - 1) / kTileN, splits);
     gemm_bf16_tn<<<grid, 128, gemm_smem_bytes(), stream>>>(g);
     return cudaGetLastError();

@@ -101,6 +101,8 @@ def lib() -> ctypes.CDLL:
     L.kwg_fd1d_price_device.restype = i32
     L.kwg_fd1d_price_uneven.argtypes = [vp, vp, vp, vp, sz, ctypes.POINTER(Fd1dParams), dp, dp]
     L.kwg_fd1d_price_uneven.restype = i32
+    L.kwg_selftest_waits.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
+    L.kwg_selftest_waits.restype = i32
     L.kwg_autotune.argtypes = [vp, ctypes.POINTER(Fd1dParams), sz, ctypes.POINTER(ctypes.c_double),
                                ctypes.POINTER(ctypes.c_double)]
     L.kwg_autotune.restype = i32
@@ -176,6 +178,14 @@ class Context:
         if rc:
             raise RuntimeError(self.last_error())
         return (ms.value, cnt.value, nb.value) if with_bytes else (ms.value, cnt.value)
+
+    def selftest_waits(self):
+        """(timed_out, completed) of the bounded-wait self-test; (1, 1) is correct."""
+        a, b = ctypes.c_int32(-1), ctypes.c_int32(-1)
+        rc = self._L.kwg_selftest_waits(self.ptr, ctypes.byref(a), ctypes.byref(b))
+        if rc:
+            raise RuntimeError(self.last_error())
+        return a.value, b.value
 
     def autotune(self, params: Fd1dParams, m: int):
         """Times the FP64 solvers on a synthetic batch of m options; records the faster
