@@ -41,8 +41,8 @@ X_DIM = T_DIM = 1024
 SCALE = 5.0
 DENSITY = math.inf  # uniform grid
 WORKLOAD = "fd1d_american_32768x1024x1024"
-# The reference's own FD64 number for this exact shape (log/z800_1024_32768.log:87-93,
-# GTX 1070): 32768 options per 39,901.747 ms.
+# The reference's own published FD64 number for this exact shape (its benchmark log
+# log/z800_1024_32768.log:87-93, GTX 1070): 32768 options per 39,901.747 ms.
 REF_PUBLISHED_OPS = 32768 / 39.901747
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
