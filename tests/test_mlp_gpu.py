@@ -329,3 +329,30 @@ def test_fused_price_matches_layer_path(net, n):
     got = d_p.cpu().numpy()
     assert np.array_equal(d_in.cpu().numpy(), d_in2.cpu().numpy())
     assert np.max(np.abs(got - want) / o["k"]) <= 1e-12
+
+
+def test_committed_weights_meet_the_error_target(ctx, built):
+    """The shipped network (kwinto-cuda_gb300/surrogate_weights.npz, trained by
+    train_surrogate.py on 2M FD64 prices at 1024 x 1024) on 8192 fresh options of the
+    same distributions: p99 absolute error vs FD64 at 1024 x 1024 within 1e-3."""
+    import os
+
+    import torch
+
+    import kwg
+    import portfolio
+
+    path = os.path.join(os.path.dirname(kwg.__file__), "surrogate_weights.npz")
+    s = kwg.Surrogate(0)
+    s.load(path)
+    o = portfolio.config1_like(8192, seed=31337)
+    fd = _fd_prices(ctx, o, t_dim=1024, x_dim=1024, scale=5.0, density=math.inf)
+    d_o = torch.from_numpy(o.view(np.uint8).copy()).cuda()
+    d_p = torch.empty(len(o), dtype=torch.float64, device="cuda")
+    d_in = torch.empty(len(o), dtype=torch.uint8, device="cuda")
+    s.price_device(d_o.data_ptr(), len(o), d_p.data_ptr(), d_in.data_ptr())
+    torch.cuda.synchronize()
+    s.close()
+    assert d_in.cpu().numpy().all()
+    err = np.abs(d_p.cpu().numpy() - fd)
+    assert np.quantile(err, 0.99) <= 1e-3, np.quantile(err, 0.99)
