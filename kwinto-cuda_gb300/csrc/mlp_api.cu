@@ -50,11 +50,10 @@ struct kwg_mlp {
     __nv_bfloat16 *dy = nullptr, *dyt = nullptr, *dz = nullptr, *dzt = nullptr;
     double* loss = nullptr;
     int* error = nullptr;
-    // surrogate pricing buffers (grow-only)
-    kwg_option* d_opts = nullptr;
-    double* d_prices = nullptr;
-    uint8_t* d_inside = nullptr;
-    size_t price_cap = 0;
+    // surrogate pricing arena (grow-only), carved by route_layout()
+    char* d_arena = nullptr;
+    size_t arena_bytes = 0;
+    char* h_arena = nullptr;  // pinned: counters and audit statistics
 };
 
 namespace {
@@ -242,6 +241,67 @@ __global__ void scale_targets(float* t, float* f, int n, float s)
     if (f[i] > -kwg::kNoFloor) f[i] *= s;
 }
 
+// ---- surrogate routing on the device
+// Route of option i: 2 outside the training box, else 1 for a seeded audit sample
+// (splitmix64 of seed + (i + 1) * golden ratio below audit_frac * 2^64), else 0.
+__device__ __forceinline__ int32_t route_of(uint8_t inside, uint64_t seed, uint64_t i, double thresh)
+{
+    if (!inside) return 2;
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (i + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)z < thresh ? 1 : 0;
+}
+
+// Routes every option and gathers the FD ones (route > 0) into sub/sub_idx at
+// slots taken with warp-aggregated atomics; cnt[0] = FD options, cnt[1] audited,
+// cnt[2] out of the box.
+__global__ void route_gather(const kwg_option* __restrict__ opts, const uint8_t* __restrict__ inside, int n,
+                             uint64_t seed, double thresh, int32_t* __restrict__ route, kwg_option* __restrict__ sub,
+                             int32_t* __restrict__ sub_idx, int* __restrict__ cnt)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int32_t r = i < n ? route_of(inside[i], seed, (uint64_t)i, thresh) : 0;
+    if (i < n) route[i] = r;
+    // every lane of the warp reaches the ballots (lanes past n carry route 0)
+    const unsigned fd = __ballot_sync(0xffffffffu, r > 0);
+    const unsigned aud = __ballot_sync(0xffffffffu, r == 1);
+    const unsigned oob = __ballot_sync(0xffffffffu, r == 2);
+    const int lane = threadIdx.x & 31, leader = fd ? __ffs(fd) - 1 : 0;
+    int base = 0;
+    if (fd && lane == leader) base = atomicAdd(&cnt[0], __popc(fd));
+    if (lane == 0) {
+        if (aud) atomicAdd(&cnt[1], __popc(aud));
+        if (oob) atomicAdd(&cnt[2], __popc(oob));
+    }
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (r > 0) {
+        const int slot = base + __popc(fd & ((1u << lane) - 1u));
+        sub[slot] = opts[i];
+        sub_idx[slot] = i;
+    }
+}
+
+// FD prices back into the output; audit statistics (sum and max of |network - FD|
+// over audited options; the max as the ordered bits of a non-negative double);
+// options whose FD solve failed get route 3.
+__global__ void route_scatter(int m, const int32_t* __restrict__ sub_idx, const double* __restrict__ fdp,
+                              const int32_t* __restrict__ fst, int32_t* __restrict__ route,
+                              double* __restrict__ prices, double* __restrict__ stats)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    const int i = sub_idx[j];
+    if (route[i] == 1) {
+        const double e = fabs(prices[i] - fdp[j]);
+        atomicAdd(&stats[0], e);
+        atomicMax(reinterpret_cast<unsigned long long*>(&stats[1]), (unsigned long long)__double_as_longlong(e));
+    }
+    prices[i] = fdp[j];
+    if (fst[j] != KWG_STATUS_OK) route[i] = 3;
+}
+
 }  // namespace
 
 extern "C" {
@@ -305,9 +365,10 @@ void kwg_mlp_destroy(kwg_mlp* h)
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     free_ws(h);
-    void* bufs[] = {h->p, h->g, h->m, h->v, h->wb, h->wt, h->loss, h->error, h->d_opts, h->d_prices, h->d_inside};
+    void* bufs[] = {h->p, h->g, h->m, h->v, h->wb, h->wt, h->loss, h->error, h->d_arena};
     for (void* b : bufs)
         if (b) cudaFree(b);
+    if (h->h_arena) cudaFreeHost(h->h_arena);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -489,7 +550,11 @@ int kwg_mlp_price_device(kwg_mlp* h, const kwg_option* d_opts, int n, double* d_
     return check_error(h);
 }
 
-// Surrogate pricing with FD fallback and audit (host arrays in and out).
+// Surrogate pricing with FD fallback and audit (host arrays in and out).  On the
+// device: network prices (fused kernel), routing and gathering of the FD options,
+// the FD solve (kwg_fd1d_price_device on the same stream), scatter and audit
+// statistics; the host copies options in, reads the FD count once, and copies
+// prices, routes and statistics out.
 int kwg_surrogate_price(kwg_ctx* ctx, kwg_mlp* h, const kwg_option* opts, size_t n, const kwg_fd1d_params* fd,
                         double audit_frac, uint64_t seed, double* prices, int32_t* route, kwg_audit* audit)
 {
@@ -498,67 +563,62 @@ int kwg_surrogate_price(kwg_ctx* ctx, kwg_mlp* h, const kwg_option* opts, size_t
         return KWG_ERR_INVALID;
     h->err.clear();
     MLP_CUDA(h, cudaSetDevice(h->device));
-    if (n > h->price_cap) {
-        if (h->d_opts) cudaFree(h->d_opts);
-        if (h->d_prices) cudaFree(h->d_prices);
-        if (h->d_inside) cudaFree(h->d_inside);
-        h->d_opts = nullptr;
-        h->d_prices = nullptr;
-        h->d_inside = nullptr;
-        h->price_cap = 0;
-        MLP_CUDA(h, cudaMalloc(&h->d_opts, n * sizeof(kwg_option)));
-        MLP_CUDA(h, cudaMalloc(&h->d_prices, n * sizeof(double)));
-        MLP_CUDA(h, cudaMalloc(&h->d_inside, n));
-        h->price_cap = n;
+    // arena: opts | prices | inside | route | sub | sub_idx | sub prices | sub status | counters | stats
+    auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t o_opts = 0, o_prices = o_opts + al(n * sizeof(kwg_option)), o_inside = o_prices + al(n * 8),
+                 o_route = o_inside + al(n), o_sub = o_route + al(n * 4), o_subidx = o_sub + al(n * sizeof(kwg_option)),
+                 o_subp = o_subidx + al(n * 4), o_subs = o_subp + al(n * 8), o_cnt = o_subs + al(n * 4),
+                 o_stats = o_cnt + 256, total = o_stats + 256;
+    if (total > h->arena_bytes) {
+        if (h->d_arena) cudaFree(h->d_arena);
+        h->d_arena = nullptr;
+        h->arena_bytes = 0;
+        MLP_CUDA(h, cudaMalloc(&h->d_arena, total));
+        h->arena_bytes = total;
     }
-    MLP_CUDA(h, cudaMemcpyAsync(h->d_opts, opts, n * sizeof(kwg_option), cudaMemcpyHostToDevice, h->stream));
-    if (int rc = kwg_mlp_price_device(h, h->d_opts, (int)n, h->d_prices, h->d_inside)) return rc;
-    std::vector<uint8_t> inside(n);
-    MLP_CUDA(h, cudaMemcpyAsync(prices, h->d_prices, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    MLP_CUDA(h, cudaMemcpyAsync(inside.data(), h->d_inside, n, cudaMemcpyDeviceToHost, h->stream));
-    MLP_CUDA(h, cudaStreamSynchronize(h->stream));
-    // route: out of the training box -> FD (2); a seeded random audit fraction -> FD (1)
-    std::vector<kwg_option> sub;
-    std::vector<size_t> where;
-    std::vector<int32_t> how;
+    if (!h->h_arena) MLP_CUDA(h, cudaMallocHost(&h->h_arena, 512));
+    char* A = h->d_arena;
+    kwg_option* d_opts = (kwg_option*)(A + o_opts);
+    double* d_prices = (double*)(A + o_prices);
+    uint8_t* d_inside = (uint8_t*)(A + o_inside);
+    int32_t* d_route = (int32_t*)(A + o_route);
+    kwg_option* d_sub = (kwg_option*)(A + o_sub);
+    int32_t* d_subidx = (int32_t*)(A + o_subidx);
+    double* d_subp = (double*)(A + o_subp);
+    int32_t* d_subs = (int32_t*)(A + o_subs);
+    int* d_cnt = (int*)(A + o_cnt);
+    double* d_stats = (double*)(A + o_stats);
+    MLP_CUDA(h, cudaMemcpyAsync(d_opts, opts, n * sizeof(kwg_option), cudaMemcpyHostToDevice, h->stream));
+    MLP_CUDA(h, cudaMemsetAsync(d_cnt, 0, 512, h->stream));  // counters and statistics
+    MLP_CUDA(h, kwg::mlp_launch_price_fused(d_opts, (int)n, h->box, h->wb, h->p, h->y_scale, d_prices, d_inside,
+                                            h->error, h->sms, h->stream));
     const double thresh = audit_frac * 18446744073709551616.0;
-    for (size_t i = 0; i < n; ++i) {
-        uint64_t z = seed + 0x9E3779B97F4A7C15ull * (i + 1);
-        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-        z ^= z >> 31;
-        const int r = !inside[i] ? 2 : ((double)z < thresh) ? 1 : 0;
-        if (route) route[i] = r;
-        if (r) {
-            sub.push_back(opts[i]);
-            where.push_back(i);
-            how.push_back(r);
-        }
-    }
+    route_gather<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(d_opts, d_inside, (int)n, seed, thresh, d_route,
+                                                                     d_sub, d_subidx, d_cnt);
+    int* hc = (int*)h->h_arena;
+    MLP_CUDA(h, cudaMemcpyAsync(hc, d_cnt, 3 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    MLP_CUDA(h, cudaStreamSynchronize(h->stream));
+    const int m = hc[0];
     kwg_audit a = {};
-    if (!sub.empty()) {
-        std::vector<double> fdp(sub.size());
-        std::vector<int32_t> fst(sub.size());
+    a.audited = hc[1];
+    a.out_of_box = hc[2];
+    if (m > 0) {
         kwg_fd1d_params q = *fd;
         q.strict = 0;
-        if (int rc = kwg_fd1d_price(ctx, sub.data(), sub.size(), &q, fdp.data(), fst.data())) {
+        if (int rc = kwg_fd1d_price_device(ctx, d_sub, (size_t)m, &q, d_subp, d_subs, h->stream)) {
             h->err = std::string("kwg_surrogate_price: FD fallback: ") + kwg_last_error(ctx);
             return rc;
         }
-        for (size_t j = 0; j < sub.size(); ++j) {
-            const size_t i = where[j];
-            if (how[j] == 1) {
-                const double e = std::fabs(prices[i] - fdp[j]);
-                a.audited += 1;
-                a.audit_abs_sum += e;
-                if (e > a.audit_abs_max) a.audit_abs_max = e;
-            } else {
-                a.out_of_box += 1;
-            }
-            prices[i] = fdp[j];
-            if (fst[j] != KWG_STATUS_OK && route) route[i] = 3;
-        }
+        route_scatter<<<(unsigned)((m + 255) / 256), 256, 0, h->stream>>>(m, d_subidx, d_subp, d_subs, d_route,
+                                                                          d_prices, d_stats);
     }
+    MLP_CUDA(h, cudaMemcpyAsync(prices, d_prices, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (route) MLP_CUDA(h, cudaMemcpyAsync(route, d_route, n * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    double* hs = (double*)(h->h_arena + 256);
+    MLP_CUDA(h, cudaMemcpyAsync(hs, d_stats, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (int rc = check_error(h)) return rc;  // synchronises the stream
+    a.audit_abs_sum = hs[0];
+    a.audit_abs_max = hs[1];
     if (audit) *audit = a;
     return KWG_OK;
 }
