@@ -328,6 +328,12 @@ def run_ours(args):
     d_prices = torch.empty(N_OPTIONS, dtype=torch.float64, device=dev)
     d_status = torch.empty(N_OPTIONS, dtype=torch.int32, device=dev)
 
+    # ---------------------------------------------------------------- autotuner: launch shapes
+    # options per block and Thomas vs PCR (FP64), threads per option (FP32), on this shape
+    tune64 = ctx.autotune_ex(prm, N_OPTIONS).as_dict()
+    tune32 = ctx.autotune_ex(kwg.params(t_dim=T_DIM, x_dim=X_DIM, scale=SCALE, density=DENSITY,
+                                        precision=kwg.FP32), N_OPTIONS).as_dict()
+
     def step(params=prm):
         rc = ctx.fd1d_price_device(d_opts.data_ptr(), N_OPTIONS, params, d_prices.data_ptr(), d_status.data_ptr(),
                                    stream.cuda_stream)
@@ -438,8 +444,10 @@ def run_ours(args):
     if not args.no_uneven:
         o3, xd3, td3 = portfolio.config3(131072, seed=42, start=rank * 131072)
         ns3 = int((xd3.astype(np.int64) * (td3.astype(np.int64) - 1)).sum())
+        uneven["tuning"] = {}
         for name, prec in (("fp64", kwg.FP64), ("fp32", kwg.FP32)):
             p3 = kwg.params(scale=SCALE, density=DENSITY, precision=prec)
+            uneven["tuning"][name] = ctx.autotune_uneven(o3, xd3, td3, p3).as_dict()
             for _ in range(max(1, args.warmup)):
                 rc, pr3, st3 = ctx.fd1d_price_uneven(o3, xd3, td3, p3)  # first call captures the graph
             barrier()
@@ -508,10 +516,7 @@ def run_ours(args):
             config4["fd64_max_rel_err_vs_oracle"] = float(np.max(np.abs(p64_[idx] - want4) / np.abs(want4)))
             config4["oracle_sample"] = len(idx)
 
-    # ---------------------------------------------------------------- autotuner on this shape
-    t_ms, p_ms = ctx.autotune(prm, N_OPTIONS)
-    tuned = {"thomas_solve_ms": t_ms, "pcr_solve_ms": p_ms, "pick": "thomas" if (p_ms < 0 or t_ms <= p_ms)
-             else "pcr"}
+    tuned = {"fp64": tune64, "fp32": tune32, "uneven_config3": uneven.pop("tuning", None)}
 
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -547,7 +552,8 @@ def run_ours(args):
         "dtype": "f64",
         "data": "synthetic (seeded splitmix64, config-2 distributions)",
         "config": {"workload": WORKLOAD, "options_per_batch": N_OPTIONS, "x_dim": X_DIM, "t_dim": T_DIM,
-                   "theta": 0.5, "scale": SCALE, "grid": "uniform", "precision": "fp64", "solver": "thomas",
+                   "theta": 0.5, "scale": SCALE, "grid": "uniform", "precision": "fp64",
+                   "solver": tune64["solver"], "block_warps": tune64["block_warps"],
                    "l2": "working set 2.7 GB per step > 129 MB L2 (no flush needed)"},
         "e2e": {"value": e2e_value, "unit": "options/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
@@ -576,7 +582,7 @@ def run_ours(args):
                                             "uniform grids, scale 5; kwg_fd1d_price_uneven (host API, CUDA graph)"),
                      "fd1d_bs_config2": fd1d_bs,
                      "precision_config4": config4,
-                     "autotune_config2_shape": tuned,
+                     "autotune": tuned,
                      "surrogate_config5": surrogate},
     }
     print(json.dumps(line), flush=True)

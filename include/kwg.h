@@ -80,6 +80,11 @@ typedef struct kwg_fd1d_params {
                           the device by (t,r,q,z,e,w) like the host path (one stream
                           synchronisation reads the PDE count); 0 (default) solves every
                           option as its own PDE, fully asynchronously */
+    int32_t block_warps;  /* FP64 streaming solver: warps (32 options each) per thread
+                             block, 1, 2 or 4; 0 (default) = tuned or 1 */
+    int32_t option_warps; /* warp-per-PDE FP32 solver: warps (32 threads each) per
+                             option, 1 or 2 (grids of more than 1024 nodes always 2);
+                             0 (default) = tuned or 1 */
 } kwg_fd1d_params;
 
 typedef struct kwg_ctx kwg_ctx;
@@ -152,12 +157,36 @@ int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const int32_t* x
                           const int32_t* t_dims, size_t n, const kwg_fd1d_params* p,
                           double* prices, int32_t* status);
 
-/* Autotuner.  Times the FP64 solvers -- thread per option (Thomas, 32 options per
- * block) and warp per option (PCR, 32 threads per option) -- on a synthetic batch
- * of m options with p's grid, and records the faster one for KWG_SOLVER_AUTO calls
- * of the same shape (precision, x_dim, t_dim, m rounded to a power of two) on this
- * context.  Writes each solver's solve time (ms; negative if not applicable).
- * No counterpart in the reference, which has one CPU solver. */
+/* Result of the autotuner: the launch shape it picked and the solve-kernel time of
+ * every candidate (-1: not timed or not applicable). */
+typedef struct kwg_tuning {
+    int32_t solver;       /* KWG_SOLVER_THOMAS or KWG_SOLVER_PCR (FP64); KWG_SOLVER_PCR (FP32) */
+    int32_t block_warps;  /* warps (32 options each) per block of the streaming FP64 solver */
+    int32_t option_warps; /* warps (32 threads each) per option of the FP32 solver */
+    int32_t reserved;
+    double thomas_ms[3];  /* streaming FP64 solver with 1, 2, 4 warps per block */
+    double pcr_ms;        /* FP64 warp-per-PDE solver */
+    double fp32_ms[2];    /* FP32 solver with 1, 2 warps per option */
+} kwg_tuning;
+
+/* Autotuner (no counterpart in the reference): on a synthetic batch of m options of
+ * p's shape and precision, times options-per-block (1, 2, 4 warps of 32 per block)
+ * and Thomas vs PCR for FP64, threads-per-option (1 or 2 warps) for FP32, and records
+ * the fastest for later calls of that shape whose p leaves the choices at 0 / AUTO.
+ * `out` may be NULL. */
+int kwg_autotune_ex(kwg_ctx* ctx, const kwg_fd1d_params* p, size_t m, kwg_tuning* out);
+
+/* The same for an uneven batch (kwg_fd1d_price_uneven's arguments): times the
+ * candidates on these options and records the fastest for uneven calls of p's
+ * precision and this batch size. */
+int kwg_autotune_uneven(kwg_ctx* ctx, const kwg_option* opts, const int32_t* x_dims, const int32_t* t_dims,
+                        size_t n, const kwg_fd1d_params* p, kwg_tuning* out);
+
+/* Compact form of kwg_autotune_ex for FP64: tunes and records the same choices and
+ * writes the best streaming (Thomas) solve time over the block sizes and the
+ * warp-per-PDE (PCR) solve time (ms; negative if not applicable).  The choice is kept
+ * for calls of the same shape (precision, x_dim, t_dim, m rounded to a power of two)
+ * on this context.  No counterpart in the reference, which has one CPU solver. */
 int kwg_autotune(kwg_ctx* ctx, const kwg_fd1d_params* p, size_t m, double* thomas_ms, double* pcr_ms);
 
 /* Tensor-core GEMM used by the MLP surrogate: C[m][n] = sum_k A[m][k] B[n][k] with

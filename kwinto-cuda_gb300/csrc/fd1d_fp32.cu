@@ -578,6 +578,10 @@ void fd1d_fp32_prepare(int)
     prepare_m<8, 1>();
     prepare_m<16, 1>();
     prepare_m<32, 1>();
+    prepare_m<2, 2>();
+    prepare_m<4, 2>();
+    prepare_m<8, 2>();
+    prepare_m<16, 2>();
     prepare_m<32, 2>();
 }
 
@@ -596,14 +600,22 @@ int fd1d_fp32_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh
 {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    // grids of up to 1024 nodes: one warp per PDE; 2048: two warps of 32 nodes per lane
-    switch (fd1d_fp32_nodes_per_lane(sh.x_dim)) {
-    case 2: return launch_m<2, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
-    case 4: return launch_m<4, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
-    case 8: return launch_m<8, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
-    case 16: return launch_m<16, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
-    case 32: return launch_m<32, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
-    case 64: return launch_m<32, 2>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    // one warp per PDE (M = nodes per lane of a 32-lane layout) or, when asked and the
+    // grid has at least 4 nodes per lane, two warps of M/2 nodes per lane; grids of
+    // 1025..2048 nodes always take two warps of 32 nodes per lane
+    const int m1 = fd1d_fp32_nodes_per_lane(sh.x_dim);
+    const bool two = m1 == 64 || (sh.option_warps == 2 && m1 >= 4);
+    switch (two ? m1 / 2 : m1) {
+    case 2: return two ? launch_m<2, 2>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev)
+                       : launch_m<2, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    case 4: return two ? launch_m<4, 2>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev)
+                       : launch_m<4, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    case 8: return two ? launch_m<8, 2>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev)
+                       : launch_m<8, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    case 16: return two ? launch_m<16, 2>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev)
+                        : launch_m<16, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    case 32: return two ? launch_m<32, 2>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev)
+                        : launch_m<32, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
     default: return -1;
     }
 }

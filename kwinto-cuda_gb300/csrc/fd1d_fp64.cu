@@ -281,7 +281,9 @@ constexpr uint32_t kStageCoef = kGroup * kNodeCoefBytes;  // 3 KB
 constexpr uint32_t kStageP = kGroup * kNodePBytes;        // 1 KB
 constexpr uint32_t kStageS = kGroup * kNodeSBytes;        // 2 KB
 constexpr uint32_t kStageBytes = kStageCoef + kStageP + kStageS;
-constexpr size_t kSolveSmem = kRing * kStageBytes + kRing * sizeof(uint64_t);
+// one warp's ring and mbarriers, rounded so the next warp's stages stay aligned
+constexpr size_t kSolveSmem = (kRing * kStageBytes + kRing * sizeof(uint64_t) + 127) / 128 * 128;
+constexpr int kMaxBlockWarps = 4;
 
 struct Ring {
     unsigned char* stage;  // kRing * kStageBytes
@@ -410,8 +412,9 @@ __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileVi
 }  // namespace
 
 // Persistent: each warp takes tiles from tile_counter[0] (zeroed by the host before
-// the launch) and runs all tDim-1 steps of its 32 PDEs.  One warp per block so the
-// scheduler spreads warps evenly over the SMs.  The sweeps stream through a 4-deep
+// the launch) and runs all tDim-1 steps of its 32 PDEs.  A block holds 1, 2 or 4
+// independent warps (32 options each; each warp has its own ring); the block size is
+// a tuned launch parameter.  The sweeps stream through a 4-deep
 // ring of 4-node stages in shared memory filled by the TMA engine; V and h|f are
 // written back with ordinary 16-byte stores.  If a ring wait expires,
 // tile_counter[1] is set, the warp drains its copies in flight and leaves; the
@@ -419,13 +422,13 @@ __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileVi
 // tile_counter[2..3] accumulates (64-bit) the bytes the launch reads and writes.
 // kHalf: theta = 1/2 (c = 1).
 template <bool kHalf>
-__global__ void __launch_bounds__(32) fd1d_solve_fp64(const PdeBatch b, Fd1dShape sh, double* __restrict__ base,
-                                                      int* __restrict__ tile_counter)
+__global__ void __launch_bounds__(32 * kMaxBlockWarps)
+    fd1d_solve_fp64(const PdeBatch b, Fd1dShape sh, double* __restrict__ base, int* __restrict__ tile_counter)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     Ring ring;
-    ring.stage = smem;
-    ring.bar = reinterpret_cast<uint64_t*>(smem + kRing * kStageBytes);
+    ring.stage = smem + (size_t)(threadIdx.x >> 5) * kSolveSmem;
+    ring.bar = reinterpret_cast<uint64_t*>(ring.stage + kRing * kStageBytes);
     const int lane = threadIdx.x & 31;
     if (lane == 0) {
         for (int s = 0; s < kRing; ++s) mbar_init(&ring.bar[s], 1);
@@ -539,18 +542,27 @@ __global__ void fd1d_interp_fp64(const PdeBatch b, const AssetBatch a, Fd1dShape
     if (status) status[i] = st;
 }
 
-int fd1d_fp64_solve_blocks(int ntiles, int device)
+int fd1d_fp64_solve_blocks(int ntiles, int device, int block_warps)
 {
-    static int cached_dev = -1, cached_max = 0, cached_sms = 0;
+    // occupancy per block size (1, 2, 4 warps), cached for one device
+    static int cached_dev = -1, cached_sms = 0, cached_max[kMaxBlockWarps + 1] = {};
     if (cached_dev != device) {
         cudaDeviceGetAttribute(&cached_sms, cudaDevAttrMultiProcessorCount, device);
-        cached_max = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_max, fd1d_solve_fp64<true>, 32, kSolveSmem);
-        if (cached_max < 1) cached_max = 1;
+        for (int bw = 1; bw <= kMaxBlockWarps; bw *= 2) {
+            cudaFuncSetAttribute(fd1d_solve_fp64<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(kMaxBlockWarps * kSolveSmem));
+            cudaFuncSetAttribute(fd1d_solve_fp64<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(kMaxBlockWarps * kSolveSmem));
+            int mx = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mx, fd1d_solve_fp64<true>, 32 * bw, bw * kSolveSmem);
+            cached_max[bw] = mx < 1 ? 1 : mx;
+        }
         cached_dev = device;
     }
-    const int cap = cached_sms * cached_max;  // one warp per block, one tile per warp at most
-    return ntiles < cap ? (ntiles > 0 ? ntiles : 1) : cap;
+    const int bw = block_warps == 2 || block_warps == 4 ? block_warps : 1;
+    const int want = (ntiles + bw - 1) / bw;  // one tile per warp at most
+    const int cap = cached_sms * cached_max[bw];
+    return want < cap ? (want > 0 ? want : 1) : cap;
 }
 
 void fd1d_prepare_kernels(int device)
@@ -582,10 +594,11 @@ int fd1d_fp64_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh
     ++launches;
     cudaMemsetAsync(counters, 0, 4 * sizeof(int), stream);
     if (ev) cudaEventRecord(ev->start, stream);
+    const int bw = sh.block_warps == 2 || sh.block_warps == 4 ? sh.block_warps : 1;
     if (sh.c == 1.)
-        fd1d_solve_fp64<true><<<solve_blocks, 32, kSolveSmem, stream>>>(b, sh, work, counters);
+        fd1d_solve_fp64<true><<<solve_blocks, 32 * bw, bw * kSolveSmem, stream>>>(b, sh, work, counters);
     else
-        fd1d_solve_fp64<false><<<solve_blocks, 32, kSolveSmem, stream>>>(b, sh, work, counters);
+        fd1d_solve_fp64<false><<<solve_blocks, 32 * bw, bw * kSolveSmem, stream>>>(b, sh, work, counters);
     if (ev) {
         cudaEventRecord(ev->stop, stream);
         if (ev->bytes) cudaMemcpyAsync(ev->bytes, counters + 2, sizeof(unsigned long long), cudaMemcpyDeviceToHost,

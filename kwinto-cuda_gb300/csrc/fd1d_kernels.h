@@ -58,6 +58,10 @@ struct Fd1dShape {
     // per-PDE shapes only: every PDE of the launch has x_dim == 32 x its nodes per
     // lane (no padded nodes), which the warp-per-PDE uniform-grid kernels require
     bool full_lanes = false;
+    // resolved launch shapes: warps per block of the streaming FP64 solver (1, 2, 4;
+    // 32 options each) and warps per option of the FP32 solver (1, 2)
+    int block_warps = 1;
+    int option_warps = 1;
 };
 
 __host__ __device__ inline int shape_x(const Fd1dShape& sh, int pde) { return sh.pde_x ? sh.pde_x[pde] : sh.x_dim; }
@@ -111,7 +115,8 @@ void fd1d_prepare_kernels(int device);
 void fd1d_fp32_prepare(int device);
 void fd1d_pcr64_prepare(int device);
 
-// Occupancy-derived persistent grid size for the FP64 solve kernel.
-int fd1d_fp64_solve_blocks(int ntiles, int device);
+// Occupancy-derived persistent grid size (blocks of block_warps warps) for the FP64
+// solve kernel.
+int fd1d_fp64_solve_blocks(int ntiles, int device, int block_warps = 1);
 
 }  // namespace kwg

@@ -235,26 +235,27 @@ __global__ void selftest_waits(int32_t* __restrict__ out, uint32_t limit)
     out[1] = kwg::mbar_wait_n(&bar[1], 0, limit) ? 1 : 0;
 }
 
-uint64_t shape_key(int precision, int x_dim, int t_dim, int m)
-{
-    int mb = 0;
-    while ((1 << mb) < m && mb < 40) ++mb;
-    return ((uint64_t)precision << 60) | ((uint64_t)(x_dim & 0xfffff) << 40) | ((uint64_t)(t_dim & 0xfffff) << 20) |
-           (uint64_t)mb;
-}
 
-// Solver for an FP64 batch: explicit choice, the autotuned one, else a cost model.
-// The thread-per-option kernel runs m/32 warps; the warp-per-option kernel runs m
-// warps at twice the FP64 work per node-step, so it wins while m/32 warps cannot
-// fill the GPU (a few warps per SM).
-int choose_solver(kwg_ctx* ctx, const kwg_fd1d_params* p, int m)
+// Launch choices for a batch of m PDEs: the explicit ones in p, else what the
+// autotuner recorded for the shape, else defaults.  FP64 solver default: a cost
+// model -- the thread-per-option kernel runs m/32 warps, the warp-per-option kernel
+// m warps at twice the FP64 work per node-step, so the latter wins while m/32 warps
+// cannot fill the GPU (a few warps per SM).
+kwg_ctx::Tuned choose(kwg_ctx* ctx, const kwg_fd1d_params* p, int m)
 {
-    if (p->precision == KWG_FP32) return KWG_SOLVER_PCR;
-    if (p->solver != KWG_SOLVER_AUTO) return p->solver;
-    const bool pcr_ok = kwg::fd1d_pcr64_nodes_per_lane(p->x_dim) > 0;
-    auto it = ctx->tuned.find(shape_key(p->precision, p->x_dim, p->t_dim, m));
-    if (it != ctx->tuned.end()) return it->second;
-    return (pcr_ok && m < 8192) ? KWG_SOLVER_PCR : KWG_SOLVER_THOMAS;
+    kwg_ctx::Tuned t;
+    auto it = ctx->tuned.find(tune_key(p->precision, p->x_dim, p->t_dim, m));
+    if (it != ctx->tuned.end()) {
+        t = it->second;
+    } else {
+        const bool pcr_ok = kwg::fd1d_pcr64_nodes_per_lane(p->x_dim) > 0;
+        t.solver = (pcr_ok && m < 8192) ? KWG_SOLVER_PCR : KWG_SOLVER_THOMAS;
+    }
+    if (p->precision == KWG_FP32) t.solver = KWG_SOLVER_PCR;
+    else if (p->solver != KWG_SOLVER_AUTO) t.solver = p->solver;
+    if (p->block_warps) t.block_warps = p->block_warps;
+    if (p->option_warps) t.option_warps = p->option_warps;
+    return t;
 }
 
 int run_batch(kwg_ctx* ctx, char* io, const IoLayout& L, int m, int n, const kwg_fd1d_params* p,
@@ -275,9 +276,11 @@ int run_batch(kwg_ctx* ctx, char* io, const IoLayout& L, int m, int n, const kwg
     a.k = (const double*)(io + L.k);
     a.pde = (const int32_t*)(io + L.pde);
     a.n = n;
-    const kwg::Fd1dShape sh = make_shape(p);
-
-    const int solver = choose_solver(ctx, p, m);
+    kwg::Fd1dShape sh = make_shape(p);
+    const kwg_ctx::Tuned tn = choose(ctx, p, m);
+    const int solver = tn.solver;
+    sh.block_warps = tn.block_warps;
+    sh.option_warps = tn.option_warps;
     if (p->precision == KWG_FP64 && solver == KWG_SOLVER_PCR) {
         const size_t wbytes = kwg::fd1d_fp32_work_bytes(m, sh.x_dim);
         if (int rc = ensure_device(ctx, &ctx->d_work, &ctx->work_bytes, wbytes)) return rc;
@@ -297,7 +300,7 @@ int run_batch(kwg_ctx* ctx, char* io, const IoLayout& L, int m, int n, const kwg
     } else {
         const size_t wbytes = kwg::fd1d_fp64_work_bytes(m_pad, sh.x_dim);
         if (int rc = ensure_device(ctx, &ctx->d_work, &ctx->work_bytes, wbytes)) return rc;
-        const int blocks = kwg::fd1d_fp64_solve_blocks(m_pad / kwg::kTile, ctx->device);
+        const int blocks = kwg::fd1d_fp64_solve_blocks(m_pad / kwg::kTile, ctx->device, sh.block_warps);
         ctx->launches += kwg::fd1d_fp64_launch(b, a, sh, (double*)ctx->d_work, (int32_t*)(io + L.pde_status),
                                                ctx->d_counter, prices, status, blocks, stream, ctx->next_events());
     }
@@ -470,6 +473,20 @@ int price_device_dedup(kwg_ctx* ctx, const kwg_option* d_opts, size_t n, size_t 
     return run_batch(ctx, io, L, m, (int)n, p, d_prices, d_status, stream);
 }
 
+// Synthetic batch of m options for the autotuner: puts and calls, strikes 80..120,
+// vols 0.1..0.6, maturities 0.25..2.
+std::vector<kwg_option> tuning_batch(size_t m)
+{
+    std::vector<kwg_option> opts(m);
+    for (size_t i = 0; i < m; ++i) {
+        const double u = (double)((i * 2654435761u) % 1000) / 1000.;
+        const double v = (double)((i * 40503u + 17) % 997) / 997.;
+        opts[i] = kwg_option{0.25 + 1.75 * v, 80. + 40. * u, 0.1 + 0.5 * (1. - u), 0.05, 0.02, 100., 1,
+                             (int8_t)((i & 1) ? 1 : -1)};
+    }
+    return opts;
+}
+
 }  // namespace
 
 
@@ -487,6 +504,8 @@ void kwg_fd1d_params_default(kwg_fd1d_params* p)
     p->solver = KWG_SOLVER_AUTO;
     p->strict = 0;
     p->device_dedup = 0;
+    p->block_warps = 0;
+    p->option_warps = 0;
 }
 
 kwg_ctx* kwg_create(int device)
@@ -587,47 +606,37 @@ int kwg_selftest_waits(kwg_ctx* ctx, int32_t* timed_out, int32_t* completed)
     return KWG_OK;
 }
 
-int kwg_autotune(kwg_ctx* ctx, const kwg_fd1d_params* p, size_t m, double* thomas_ms, double* pcr_ms)
+int kwg_autotune_ex(kwg_ctx* ctx, const kwg_fd1d_params* p, size_t m, kwg_tuning* out)
 {
     if (!ctx) return KWG_ERR_INVALID;
     ctx->err.clear();
     if (int rc = check_params(ctx, p)) return rc;
+    if (m == 0 || m > (size_t)INT32_MAX / 4) return set_err(ctx, KWG_ERR_INVALID, "kwg_autotune: bad batch size");
+    const std::vector<kwg_option> opts = tuning_batch(m);
+    std::vector<double> prices(m);
+    const bool pcr_ok = kwg::fd1d_pcr64_nodes_per_lane(p->x_dim) > 0;
+    const kwg_ctx::Tuned best = tune(ctx, p, pcr_ok, [&](const kwg_fd1d_params& q) {
+        return kwg_fd1d_price(ctx, opts.data(), m, &q, prices.data(), nullptr);
+    }, out);
+    ctx->tuned[tune_key(p->precision, p->x_dim, p->t_dim, (int)m)] = best;
+    ctx->err.clear();
+    return KWG_OK;
+}
+
+int kwg_autotune(kwg_ctx* ctx, const kwg_fd1d_params* p, size_t m, double* thomas_ms, double* pcr_ms)
+{
     if (thomas_ms) *thomas_ms = -1.;
     if (pcr_ms) *pcr_ms = -1.;
-    if (m == 0 || m > (size_t)INT32_MAX / 2) return set_err(ctx, KWG_ERR_INVALID, "kwg_autotune: bad batch size");
-    if (p->precision != KWG_FP64) return KWG_OK;  // FP32 has one solver
-    // synthetic batch: puts and calls, strikes 80..120, vols 0.1..0.6, maturities 0.25..2
-    std::vector<kwg_option> opts(m);
-    for (size_t i = 0; i < m; ++i) {
-        const double u = (double)((i * 2654435761u) % 1000) / 1000.;
-        const double v = (double)((i * 40503u + 17) % 997) / 997.;
-        opts[i] = kwg_option{0.25 + 1.75 * v, 80. + 40. * u, 0.1 + 0.5 * (1. - u), 0.05, 0.02, 100., 1,
-                             (int8_t)((i & 1) ? 1 : -1)};
-    }
-    kwg_fd1d_params q = *p;
-    q.strict = 0;
-    std::vector<double> prices(m);
-    const bool was_profiling = ctx->profiling;
-    double best_ms[3] = {-1., -1., -1.};
-    for (int solver : {KWG_SOLVER_THOMAS, KWG_SOLVER_PCR}) {
-        if (solver == KWG_SOLVER_PCR && kwg::fd1d_pcr64_nodes_per_lane(p->x_dim) < 0) continue;
-        q.solver = solver;
-        if (int rc = kwg_fd1d_price(ctx, opts.data(), m, &q, prices.data(), nullptr)) return rc;  // warm-up
-        kwg_set_profiling(ctx, 1);
-        int rc = kwg_fd1d_price(ctx, opts.data(), m, &q, prices.data(), nullptr);
-        double ms = 0.;
-        int cnt = 0;
-        if (!rc) rc = kwg_profile_read(ctx, &ms, &cnt, nullptr);
-        kwg_set_profiling(ctx, was_profiling);
-        if (rc) return rc;
-        best_ms[solver] = ms;
-    }
-    if (thomas_ms) *thomas_ms = best_ms[KWG_SOLVER_THOMAS];
-    if (pcr_ms) *pcr_ms = best_ms[KWG_SOLVER_PCR];
-    const int pick = (best_ms[KWG_SOLVER_PCR] >= 0. && best_ms[KWG_SOLVER_PCR] < best_ms[KWG_SOLVER_THOMAS])
-                         ? KWG_SOLVER_PCR
-                         : KWG_SOLVER_THOMAS;
-    ctx->tuned[shape_key(p->precision, p->x_dim, p->t_dim, (int)m)] = pick;
+    if (!ctx) return KWG_ERR_INVALID;
+    if (int rc = check_params(ctx, p)) return rc;
+    if (p->precision != KWG_FP64) return KWG_OK;  // FP32 has one solver family
+    kwg_tuning t;
+    if (int rc = kwg_autotune_ex(ctx, p, m, &t)) return rc;
+    double best = -1.;
+    for (double v : t.thomas_ms)
+        if (v >= 0. && (best < 0. || v < best)) best = v;
+    if (thomas_ms) *thomas_ms = best;
+    if (pcr_ms) *pcr_ms = t.pcr_ms;
     return KWG_OK;
 }
 

@@ -34,8 +34,14 @@ struct kwg_ctx {
     cudaGraphExec_t graph_exec = nullptr;
     uint64_t graph_sig = 0;
     int graph_launches = 0;
-    // autotuner decisions: shape key -> solver (KWG_SOLVER_THOMAS or KWG_SOLVER_PCR)
-    std::map<uint64_t, int> tuned;
+    // autotuner decisions: shape key -> solver (KWG_SOLVER_THOMAS or KWG_SOLVER_PCR),
+    // warps per block of the streaming solver, warps per option of the FP32 solver
+    struct Tuned {
+        int solver = KWG_SOLVER_THOMAS;
+        int block_warps = 1;
+        int option_warps = 1;
+    };
+    std::map<uint64_t, Tuned> tuned;
     bool profiling = false;
     std::vector<kwg::SolveEvents> events;  // pool, reused across reads
     size_t events_used = 0;
@@ -121,8 +127,88 @@ inline int check_params(kwg_ctx* ctx, const kwg_fd1d_params* p)
         return set_err(ctx, KWG_ERR_INVALID, "kwg: FP32 uses the on-chip partitioned solver (KWG_SOLVER_PCR or AUTO)");
     if (p->precision == KWG_FP32 && kwg::fd1d_fp32_nodes_per_lane(p->x_dim) < 0)
         return set_err(ctx, KWG_ERR_INVALID, "kwg: FP32 stepping supports x_dim <= 2048");
+    if (p->block_warps != 0 && p->block_warps != 1 && p->block_warps != 2 && p->block_warps != 4)
+        return set_err(ctx, KWG_ERR_INVALID, "kwg: block_warps must be 0, 1, 2 or 4");
+    if (p->option_warps < 0 || p->option_warps > 2)
+        return set_err(ctx, KWG_ERR_INVALID, "kwg: option_warps must be 0, 1 or 2");
     return KWG_OK;
 }
+
+// Autotuner key: precision, grid and the batch size rounded up to a power of two.
+// Uneven batches use x_dim = t_dim = 0.
+inline uint64_t tune_key(int precision, int x_dim, int t_dim, long long m)
+{
+    int mb = 0;
+    while ((1ll << mb) < m && mb < 40) ++mb;
+    return ((uint64_t)precision << 60) | ((uint64_t)(x_dim & 0xfffff) << 40) | ((uint64_t)(t_dim & 0xfffff) << 20) |
+           (uint64_t)mb;
+}
+
+// Solve-kernel milliseconds of one call (after a warm-up call), or -1 on error.
+template <typename F>
+inline double time_solve(kwg_ctx* ctx, F&& call)
+{
+    if (call() != KWG_OK) return -1.;
+    const bool was = ctx->profiling;
+    kwg_set_profiling(ctx, 1);
+    double ms = 0.;
+    int cnt = 0;
+    int rc = call();
+    if (rc == KWG_OK) rc = kwg_profile_read(ctx, &ms, &cnt, nullptr);
+    kwg_set_profiling(ctx, was);
+    return rc == KWG_OK ? ms : -1.;
+}
+
+// Times every candidate launch shape on fn(params) and returns the fastest: FP64 --
+// the streaming solver with 1, 2, 4 warps per block and the warp-per-PDE solver
+// (when pcr_ok); FP32 -- 1 and 2 warps per option.
+template <typename F>
+inline kwg_ctx::Tuned tune(kwg_ctx* ctx, const kwg_fd1d_params* p, bool pcr_ok, F&& fn, kwg_tuning* out)
+{
+    kwg_tuning r = {};
+    for (double& v : r.thomas_ms) v = -1.;
+    r.pcr_ms = -1.;
+    r.fp32_ms[0] = r.fp32_ms[1] = -1.;
+    kwg_fd1d_params q = *p;
+    q.strict = 0;
+    kwg_ctx::Tuned best;
+    double best_ms = -1.;
+    auto consider = [&](double ms, int solver, int bw, int ow) {
+        if (ms >= 0. && (best_ms < 0. || ms < best_ms)) {
+            best_ms = ms;
+            best.solver = solver;
+            best.block_warps = bw;
+            best.option_warps = ow;
+        }
+    };
+    if (p->precision == KWG_FP64) {
+        const int bws[3] = {1, 2, 4};
+        for (int i = 0; i < 3; ++i) {
+            q.solver = KWG_SOLVER_THOMAS;
+            q.block_warps = bws[i];
+            r.thomas_ms[i] = time_solve(ctx, [&] { return fn(q); });
+            consider(r.thomas_ms[i], KWG_SOLVER_THOMAS, bws[i], 1);
+        }
+        if (pcr_ok) {
+            q.solver = KWG_SOLVER_PCR;
+            q.block_warps = 0;
+            r.pcr_ms = time_solve(ctx, [&] { return fn(q); });
+            consider(r.pcr_ms, KWG_SOLVER_PCR, 1, 1);
+        }
+    } else {
+        for (int w = 1; w <= 2; ++w) {
+            q.option_warps = w;
+            r.fp32_ms[w - 1] = time_solve(ctx, [&] { return fn(q); });
+            consider(r.fp32_ms[w - 1], KWG_SOLVER_PCR, 1, w);
+        }
+    }
+    r.solver = best.solver;
+    r.block_warps = best.block_warps;
+    r.option_warps = best.option_warps;
+    if (out) *out = r;
+    return best;
+}
+
 
 inline kwg::Fd1dShape make_shape(const kwg_fd1d_params* p)
 {

@@ -102,6 +102,21 @@ extern "C" int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const
     q.x_dim = x_max;
     q.t_dim = t_max;
     if (int rc = check_params(ctx, &q)) return rc;
+    // launch choices: the explicit ones, else what kwg_autotune_uneven recorded for
+    // uneven batches of this precision and size, else Thomas with one warp per block
+    // (FP64) and one warp per option (FP32)
+    kwg_ctx::Tuned tn;
+    {
+        const auto it = ctx->tuned.find(tune_key(q.precision, 0, 0, (long long)n));
+        if (it != ctx->tuned.end()) {
+            tn = it->second;
+            if (q.precision == KWG_FP64 && q.solver == KWG_SOLVER_AUTO &&
+                (tn.solver != KWG_SOLVER_PCR || kwg::fd1d_pcr64_nodes_per_lane(x_max) > 0))
+                q.solver = tn.solver;
+        }
+        if (q.block_warps) tn.block_warps = q.block_warps;
+        if (q.option_warps) tn.option_warps = q.option_warps;
+    }
     const bool pcr = q.precision == KWG_FP32 || q.solver == KWG_SOLVER_PCR;
     KWG_CUDA(ctx, cudaSetDevice(ctx->device));
 
@@ -244,6 +259,8 @@ extern "C" int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const
     a.pde = (const int32_t*)(io + L.pde);
     a.n = (int)n;
     kwg::Fd1dShape sh = make_shape(&q);
+    sh.block_warps = tn.block_warps;
+    sh.option_warps = tn.option_warps;
     sh.pde_x = (const int32_t*)(io + L.px);
     sh.pde_t = (const int32_t*)(io + L.pt);
     if (!pcr) {
@@ -260,7 +277,7 @@ extern "C" int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const
         int launches = 0;
         cudaMemcpyAsync(ctx->d_io, ctx->h_io, L.in_bytes, cudaMemcpyHostToDevice, st);
         if (!pcr) {
-            const int blocks = kwg::fd1d_fp64_solve_blocks((int)tiles.size(), ctx->device);
+            const int blocks = kwg::fd1d_fp64_solve_blocks((int)tiles.size(), ctx->device, sh.block_warps);
             launches += kwg::fd1d_fp64_launch(b, a, sh, (double*)ctx->d_work, d_pde_status, ctx->d_counter, d_prices,
                                               d_status, blocks, st, ctx->next_events());
         } else {
@@ -301,7 +318,8 @@ extern "C" int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const
     };
 
     uint64_t sig = 0x5eed;
-    for (uint64_t v : {(uint64_t)q.precision, (uint64_t)pcr, (uint64_t)n, (uint64_t)ms, (uint64_t)tiles.size(),
+    for (uint64_t v : {(uint64_t)q.precision, (uint64_t)pcr, (uint64_t)sh.block_warps, (uint64_t)sh.option_warps,
+                       (uint64_t)n, (uint64_t)ms, (uint64_t)tiles.size(),
                        (uint64_t)node_lanes, (uint64_t)(uintptr_t)ctx->d_io, (uint64_t)(uintptr_t)ctx->d_work,
                        (uint64_t)(uintptr_t)ctx->h_io})
         sig = mix(sig, v);
@@ -359,5 +377,24 @@ extern "C" int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const
             return set_err(ctx, hs[i] == KWG_STATUS_OUT_OF_GRID ? KWG_ERR_OUT_OF_GRID : KWG_ERR_SOLVER, msg);
         }
     }
+    return KWG_OK;
+}
+
+extern "C" int kwg_autotune_uneven(kwg_ctx* ctx, const kwg_option* opts, const int32_t* x_dims,
+                                   const int32_t* t_dims, size_t n, const kwg_fd1d_params* p, kwg_tuning* out)
+{
+    if (!ctx) return KWG_ERR_INVALID;
+    ctx->err.clear();
+    if (!p || !opts || !x_dims || !t_dims || n == 0 || n > (size_t)INT32_MAX / 4)
+        return set_err(ctx, KWG_ERR_INVALID, "kwg_autotune_uneven: bad arguments");
+    int x_max = 0;
+    for (size_t i = 0; i < n; ++i) x_max = std::max(x_max, (int)x_dims[i]);
+    std::vector<double> prices(n);
+    const bool pcr_ok = kwg::fd1d_pcr64_nodes_per_lane(x_max) > 0;
+    const kwg_ctx::Tuned best = tune(ctx, p, pcr_ok, [&](const kwg_fd1d_params& q) {
+        return kwg_fd1d_price_uneven(ctx, opts, x_dims, t_dims, n, &q, prices.data(), nullptr);
+    }, out);
+    ctx->tuned[tune_key(p->precision, 0, 0, (long long)n)] = best;
+    ctx->err.clear();
     return KWG_OK;
 }

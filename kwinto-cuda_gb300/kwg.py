@@ -53,6 +53,8 @@ class Fd1dParams(ctypes.Structure):
         ("solver", ctypes.c_int32),
         ("strict", ctypes.c_int32),
         ("device_dedup", ctypes.c_int32),
+        ("block_warps", ctypes.c_int32),
+        ("option_warps", ctypes.c_int32),
     ]
 
 
@@ -70,6 +72,26 @@ class Audit(ctypes.Structure):
 MLP_WIDTH, MLP_LAYERS, MLP_IN = 128, 5, 5
 MLP_PARAMS = MLP_LAYERS * MLP_WIDTH * MLP_WIDTH + MLP_LAYERS * MLP_WIDTH
 ROUTE_NETWORK, ROUTE_AUDIT, ROUTE_OUT_OF_BOX, ROUTE_FD_FAILED = 0, 1, 2, 3
+
+class Tuning(ctypes.Structure):
+    """struct kwg_tuning (include/kwg.h)."""
+
+    _fields_ = [
+        ("solver", ctypes.c_int32),
+        ("block_warps", ctypes.c_int32),
+        ("option_warps", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("thomas_ms", ctypes.c_double * 3),
+        ("pcr_ms", ctypes.c_double),
+        ("fp32_ms", ctypes.c_double * 2),
+    ]
+
+    def as_dict(self) -> dict:
+        return {"solver": {SOLVER_THOMAS: "thomas", SOLVER_PCR: "pcr"}.get(self.solver, self.solver),
+                "block_warps": self.block_warps, "option_warps": self.option_warps,
+                "thomas_ms_by_block_warps": {1: self.thomas_ms[0], 2: self.thomas_ms[1], 4: self.thomas_ms[2]},
+                "pcr_ms": self.pcr_ms, "fp32_ms_by_option_warps": {1: self.fp32_ms[0], 2: self.fp32_ms[1]}}
+
 
 _lib = None
 
@@ -101,6 +123,10 @@ def lib() -> ctypes.CDLL:
     L.kwg_fd1d_price_device.restype = i32
     L.kwg_fd1d_price_uneven.argtypes = [vp, vp, vp, vp, sz, ctypes.POINTER(Fd1dParams), dp, dp]
     L.kwg_fd1d_price_uneven.restype = i32
+    L.kwg_autotune_ex.argtypes = [vp, ctypes.POINTER(Fd1dParams), sz, ctypes.POINTER(Tuning)]
+    L.kwg_autotune_ex.restype = i32
+    L.kwg_autotune_uneven.argtypes = [vp, vp, vp, vp, sz, ctypes.POINTER(Fd1dParams), ctypes.POINTER(Tuning)]
+    L.kwg_autotune_uneven.restype = i32
     L.kwg_selftest_waits.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
     L.kwg_selftest_waits.restype = i32
     L.kwg_autotune.argtypes = [vp, ctypes.POINTER(Fd1dParams), sz, ctypes.POINTER(ctypes.c_double),
@@ -195,6 +221,25 @@ class Context:
         if rc:
             raise RuntimeError(self.last_error())
         return a.value, b.value
+
+    def autotune_ex(self, params: Fd1dParams, m: int) -> Tuning:
+        """Times options-per-block and Thomas vs PCR (FP64) or threads-per-option (FP32) on
+        a synthetic batch of m options of params' shape; records and returns the choice."""
+        t = Tuning()
+        if self._L.kwg_autotune_ex(self.ptr, ctypes.byref(params), m, ctypes.byref(t)):
+            raise RuntimeError(self.last_error())
+        return t
+
+    def autotune_uneven(self, opts: np.ndarray, x_dims, t_dims, params: Fd1dParams) -> Tuning:
+        """The same on an uneven batch; the choice applies to uneven calls of its size."""
+        opts = np.ascontiguousarray(opts, dtype=OPTION_DTYPE)
+        xd = np.ascontiguousarray(x_dims, dtype=np.int32)
+        td = np.ascontiguousarray(t_dims, dtype=np.int32)
+        t = Tuning()
+        if self._L.kwg_autotune_uneven(self.ptr, opts.ctypes.data, xd.ctypes.data, td.ctypes.data, len(opts),
+                                       ctypes.byref(params), ctypes.byref(t)):
+            raise RuntimeError(self.last_error())
+        return t
 
     def fd1d_price(self, opts: np.ndarray, params: Fd1dParams):
         """Host arrays in, host arrays out. Returns (rc, prices, status)."""
@@ -498,10 +543,11 @@ class PricerFactory:
 
 
 def params(t_dim=512, x_dim=512, theta=0.5, scale=50.0, density=0.25, precision=FP64, solver=SOLVER_AUTO,
-           strict=0) -> Fd1dParams:
+           strict=0, block_warps=0, option_warps=0) -> Fd1dParams:
     p = default_params()
     p.t_dim, p.x_dim, p.theta, p.scale, p.density = t_dim, x_dim, theta, scale, density
     p.precision, p.solver, p.strict = precision, solver, strict
+    p.block_warps, p.option_warps = block_warps, option_warps
     return p
 
 

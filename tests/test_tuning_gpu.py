@@ -1,0 +1,87 @@
+"""Launch-shape knobs and the autotuner: options per block of the streaming FP64
+solver (1, 2, 4 warps of 32 options), threads per option of the FP32 solver (1 or 2
+warps), Thomas vs PCR.  Every shape must price identically (FP64 streaming: bit for
+bit, lanes do not depend on their neighbours) or within the FP32 bar."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def price(ctx, o, **kw):
+    import kwg
+
+    rc, p, st = ctx.fd1d_price(o, kwg.params(**kw))
+    assert rc == kwg.KWG_OK, ctx.last_error()
+    assert (st == 0).all()
+    return p
+
+
+@pytest.mark.parametrize("bw", [2, 4])
+def test_block_warps_are_bit_identical(ctx, bw):
+    import portfolio
+
+    o = portfolio.config1_like(3000, seed=17)  # 94 tiles: blocks with fewer warps than tiles at the tail
+    kw = dict(t_dim=96, x_dim=320, scale=5.0, density=0.25, solver=1)
+    assert np.array_equal(price(ctx, o, block_warps=bw, **kw), price(ctx, o, block_warps=1, **kw))
+
+
+@pytest.mark.parametrize("x_dim", [128, 256, 512, 1000, 1024, 2048])
+def test_fp32_two_warps_per_option(ctx, x_dim):
+    """Two warps per option (64 lanes, 5 + 1 reduction levels through shared memory)
+    against the FP64 oracle, on uniform grids (the 7-field tables) and the padded
+    1000-node grid."""
+    import kwg
+    import kwor
+    import portfolio
+
+    o = portfolio.config1_like(96, seed=x_dim)
+    dens = 0.25 if x_dim == 1000 else math.inf
+    kw = dict(t_dim=128, x_dim=x_dim, scale=5.0, density=dens)
+    p2 = price(ctx, o, precision=kwg.FP32, option_warps=2, **kw)
+    rc, msg, want, _ = kwor.fd1d_price(o, **kw)
+    assert rc == 0, msg
+    assert np.max(np.abs(p2 - want)) <= 1e-5
+
+
+def test_autotune_records_and_applies_the_choice(ctx):
+    import kwg
+    import portfolio
+
+    prm = kwg.params(t_dim=64, x_dim=256, scale=5.0, density=math.inf)
+    t = ctx.autotune_ex(prm, 4096)
+    d = t.as_dict()
+    timed = [v for v in d["thomas_ms_by_block_warps"].values() if v >= 0] + ([d["pcr_ms"]] if d["pcr_ms"] >= 0 else [])
+    assert len(timed) >= 3 and all(v > 0 for v in timed)
+    best = min(timed)
+    chosen = d["pcr_ms"] if d["solver"] == "pcr" else d["thomas_ms_by_block_warps"][d["block_warps"]]
+    assert chosen == best
+    o = portfolio.config1_like(4096, seed=2)
+    auto = price(ctx, o, t_dim=64, x_dim=256, scale=5.0, density=math.inf)
+    explicit = price(ctx, o, t_dim=64, x_dim=256, scale=5.0, density=math.inf, solver=t.solver,
+                     block_warps=t.block_warps)
+    assert np.array_equal(auto, explicit)
+    # FP32: threads per option
+    t32 = ctx.autotune_ex(kwg.params(t_dim=64, x_dim=512, scale=5.0, density=math.inf, precision=kwg.FP32), 2048)
+    assert t32.option_warps in (1, 2) and min(t32.fp32_ms) > 0
+
+
+def test_autotune_uneven(ctx):
+    import kwg
+    import portfolio
+
+    o, xd, td = portfolio.config3(3000, seed=9)
+    xd = np.minimum(xd, 1024)
+    td = np.minimum(td, 200)
+    prm = kwg.params(scale=5.0, density=math.inf)
+    t = ctx.autotune_uneven(o, xd, td, prm)
+    assert t.solver in (kwg.SOLVER_THOMAS, kwg.SOLVER_PCR) and t.block_warps in (1, 2, 4)
+    rc, auto, st = ctx.fd1d_price_uneven(o, xd, td, prm)
+    assert rc == 0
+    rc, explicit, st2 = ctx.fd1d_price_uneven(o, xd, td, kwg.params(scale=5.0, density=math.inf, solver=t.solver,
+                                                                    block_warps=t.block_warps))
+    assert rc == 0 and np.array_equal(st, st2)
+    ok = st == 0
+    assert np.array_equal(auto[ok], explicit[ok])
