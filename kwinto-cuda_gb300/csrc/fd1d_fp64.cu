@@ -392,8 +392,6 @@ __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileVi
                 rs[k] = compact ? cs : sc_[(idx * kCoef + 2) * kTile];
             }
         }
-        __syncwarp();  // stage s fully read before it is refilled
-        if (lane == 0 && g + kRing < ng) issue<kUp>(ring, v + kRing, tv, g + kRing, N, rg);
 #pragma unroll
         for (int k = 0; k < kGroup; ++k) {
             if (k < count) {
@@ -405,6 +403,10 @@ __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileVi
                 if (active) sout[(size_t)j * kTile] = make_double2(vn, f);
             }
         }
+        // refill after the stage's FMA chain is under way (the ring still runs three
+        // stages ahead); every lane read the stage into registers above
+        __syncwarp();
+        if (lane == 0 && g + kRing < ng) issue<kUp>(ring, v + kRing, tv, g + kRing, N, rg);
     }
     return true;
 }
