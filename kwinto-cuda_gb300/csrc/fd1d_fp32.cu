@@ -1,7 +1,8 @@
-// fd1d_fp32.cu -- FP32 stepping with FP64-accurate state: one warp per PDE (two for
-// grids of 1025..2048 nodes), the whole PDE on chip (state in registers, coefficient
-// tables in shared memory), a partitioned tridiagonal solve with a cyclic reduction
-// of the separator system (warp shuffles; shared memory across the warps of a PDE).
+// fd1d_fp32.cu -- FP32 stepping with FP64-accurate state: one or two warps per PDE
+// (tuned; always two for grids of 1025..2048 nodes), the whole PDE on chip (state in
+// registers, coefficient tables in shared memory), a partitioned tridiagonal solve
+// with a cyclic reduction of the separator system (warp shuffles; shared memory
+// across the warps of a PDE).
 //
 // Numerics.  The reference step B V' = E V (src/Math/kwFd1d.cpp:61-132) is taken in
 // delta form,  V' = max(V + d, p)  with  B d = dt A V  (E = B + dt A), so FP32 only
