@@ -146,7 +146,7 @@ def cpu_oracle_rate(opts_all, budget_s=12.0):
 def measured_traffic(ns):
     """DRAM bytes per solve launch from the committed ncu summary (dram__bytes_read +
     dram__bytes_write of one captured launch, per node-step), scaled to ns node-steps."""
-    path = os.path.join(ROOT, "profiles", "fd1d_solve_fp64_config2.md")
+    path = os.path.join(ROOT, "profiles", "fd1d_solve_fp64_32768x1024.md")
     try:
         for line in open(path):
             if line.startswith("traffic per full launch (bytes):"):
@@ -202,7 +202,7 @@ def run_reference(args):
     kind = "reference" if use_ref else "port"
 
     def one(i):
-        o = portfolio.config1_like(per_step, seed=42, start=(i * per_step) % N_OPTIONS)
+        o = portfolio.american_portfolio(per_step, seed=42, start=(i * per_step) % N_OPTIONS)
         t0 = time.perf_counter()
         if use_ref:
             rc, msg, _, _ = kwor.ref_price(o, density=portfolio.REFERENCE_UNIFORM_DENSITY, scale=SCALE,
@@ -226,7 +226,7 @@ def run_reference(args):
         "impl": "reference", "metric": "options_per_sec_fd64_1024x1024", "value": value, "unit": "options/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": value / REF_PUBLISHED_OPS, "dtype": "f64",
-        "data": "synthetic (seeded splitmix64, config-2 distributions)",
+        "data": "synthetic (seeded splitmix64; American, S=100, K~U[80,120], vol~U[0.1,0.6], r,q~U[0,0.1], T~U[0.25,2])",
         "config": {"workload": WORKLOAD, "options_per_batch": N_OPTIONS, "x_dim": X_DIM, "t_dim": T_DIM,
                    "theta": 0.5, "scale": SCALE, "grid": "uniform", "precision": "fp64"},
         "cpu_baseline": {"value": value, "unit": "options/s", "cores": cores, "kind": kind, "sample": sample},
@@ -256,7 +256,7 @@ def surrogate_variant(args, ctx, rank, ws, fd32_rate, barrier, max_over_ranks):
     net = kwg.Surrogate(torch.cuda.current_device())
     net.load(SURROGATE_WEIGHTS)
     meta = json.loads(str(np.load(SURROGATE_WEIGHTS)["meta"])) if "meta" in np.load(SURROGATE_WEIGHTS) else {}
-    opts = portfolio.config1_like(n, seed=5005, start=rank * n)
+    opts = portfolio.american_portfolio(n, seed=5005, start=rank * n)
     fd = kwg.params(t_dim=T_DIM, x_dim=X_DIM, scale=SCALE, density=DENSITY, precision=kwg.FP32)
     for i in range(max(1, args.warmup)):
         prices, route, audit = net.price(ctx, opts, fd, SURROGATE_AUDIT, seed=100 + i)
@@ -298,7 +298,7 @@ def surrogate_variant(args, ctx, rank, ws, fd32_rate, barrier, max_over_ranks):
             "check_sample": len(idx), "p99_abs_err_vs_fd64": float(np.quantile(err, 0.99)),
             "max_abs_err_vs_fd64": float(err.max()), "mean_abs_err_vs_fd64": float(err.mean()),
             "training": meta,
-            "workload": "1M fresh config-2-distribution options (seeded), 1% audit, FD32 fallback at "
+            "workload": "1M fresh options (seeded; S=100, K~U[80,120], vol~U[0.1,0.6], r,q~U[0,0.1], T~U[0.25,2]), 1% audit, FD32 fallback at "
                         "1024x1024; kwg_surrogate_price (host arrays, H2D/D2H inside the timing)"}
 
 
@@ -322,7 +322,7 @@ def run_ours(args):
     stream = torch.cuda.Stream(dev)
 
     # each rank prices its own batch (weak scaling), drawn from its own window of the stream
-    opts = shard.config_shard(N_OPTIONS, rank, seed=42)
+    opts = shard.portfolio_shard(N_OPTIONS, rank, seed=42)
     prm = kwg.params(t_dim=T_DIM, x_dim=X_DIM, scale=SCALE, density=DENSITY, precision=kwg.FP64)
     d_opts = torch.from_numpy(opts.view(np.uint8).copy()).to(dev)
     d_prices = torch.empty(N_OPTIONS, dtype=torch.float64, device=dev)
@@ -439,10 +439,10 @@ def run_ours(args):
         fd1d_bs["max_rel_err_vs_oracle"] = float(np.max(np.abs(pbs[idx] - wantbs) / np.abs(wantbs)))
         fd1d_bs["oracle_sample"] = len(idx)
 
-    # ---------------------------------------------------------------- uneven batch (config-3 shapes)
+    # ---------------------------------------------------------------- uneven batch (131072 options, per-option grids)
     uneven = {}
     if not args.no_uneven:
-        o3, xd3, td3 = portfolio.config3(131072, seed=42, start=rank * 131072)
+        o3, xd3, td3 = portfolio.uneven_portfolio(131072, seed=42, start=rank * 131072)
         ns3 = int((xd3.astype(np.int64) * (td3.astype(np.int64) - 1)).sum())
         uneven["tuning"] = {}
         for name, prec in (("fp64", kwg.FP64), ("fp32", kwg.FP32)):
@@ -473,14 +473,14 @@ def run_ours(args):
                 uneven[name]["max_abs_err_vs_fd64"] = float(e.max())
                 uneven[name]["p99_abs_err_vs_fd64"] = float(np.percentile(e, 99))
 
-    # ---------------------------------------------------------------- surrogate + FD32 fallback (config 5)
+    # ---------------------------------------------------------------- surrogate + FD32 fallback (1M fresh options)
     surrogate = surrogate_variant(args, ctx, rank, ws, value32, barrier, max_over_ranks) if not args.no_surrogate \
         else {"skipped": "--no-surrogate"}
 
-    # ---------------------------------------------------------------- precision study (config 4)
-    config4 = {"skipped": "--no-config4"}
-    if not args.no_config4:
-        o4 = portfolio.config1_like(65536, seed=44, start=rank * 65536)
+    # ---------------------------------------------------------------- precision study (65536 options, 2048 x 2048)
+    fine = {"skipped": "--no-fine-study"}
+    if not args.no_fine_study:
+        o4 = portfolio.american_portfolio(65536, seed=44, start=rank * 65536)
         res4 = {}
         for name, prec in (("fp64", kwg.FP64), ("fp32", kwg.FP32)):
             p4 = kwg.params(t_dim=2048, x_dim=2048, scale=SCALE, density=0.25, precision=prec)
@@ -497,7 +497,7 @@ def run_ours(args):
         ok4 = (s64_ == 0) & (s32_ == 0)
         e_abs = np.abs(p32_[ok4] - p64_[ok4])
         e_rel = e_abs / np.maximum(np.abs(p64_[ok4]), 1e-12)
-        config4 = {"options": len(o4), "x_dim": 2048, "t_dim": 2048, "density": 0.25, "scale": SCALE,
+        fine = {"options": len(o4), "x_dim": 2048, "t_dim": 2048, "density": 0.25, "scale": SCALE,
                    "fd64_options_per_sec_e2e": ws * len(o4) / t64_, "fd32_options_per_sec_e2e": ws * len(o4) / t32_,
                    "fd32_speedup": t64_ / t32_,
                    "fd32_max_abs_err_vs_fd64": float(e_abs.max()),
@@ -513,10 +513,10 @@ def run_ours(args):
             rc4, msg4, want4, _ = kwor.fd1d_price(o4[idx], t_dim=2048, x_dim=2048, scale=SCALE, density=0.25)
             if rc4 != 0:
                 raise RuntimeError(msg4)
-            config4["fd64_max_rel_err_vs_oracle"] = float(np.max(np.abs(p64_[idx] - want4) / np.abs(want4)))
-            config4["oracle_sample"] = len(idx)
+            fine["fd64_max_rel_err_vs_oracle"] = float(np.max(np.abs(p64_[idx] - want4) / np.abs(want4)))
+            fine["oracle_sample"] = len(idx)
 
-    tuned = {"fp64": tune64, "fp32": tune32, "uneven_config3": uneven.pop("tuning", None)}
+    tuned = {"fp64": tune64, "fp32": tune32, "uneven_131072": uneven.pop("tuning", None)}
 
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -550,7 +550,7 @@ def run_ours(args):
         "scaling": "weak",
         "vs_baseline": value / REF_PUBLISHED_OPS,
         "dtype": "f64",
-        "data": "synthetic (seeded splitmix64, config-2 distributions)",
+        "data": "synthetic (seeded splitmix64; American, S=100, K~U[80,120], vol~U[0.1,0.6], r,q~U[0,0.1], T~U[0.25,2])",
         "config": {"workload": WORKLOAD, "options_per_batch": N_OPTIONS, "x_dim": X_DIM, "t_dim": T_DIM,
                    "theta": 0.5, "scale": SCALE, "grid": "uniform", "precision": "fp64",
                    "solver": tune64["solver"], "block_warps": tune64["block_warps"],
@@ -577,13 +577,13 @@ def run_ours(args):
                               "max_abs_err_vs_fd64": float(err32.max()),
                               "p99_abs_err_vs_fd64": float(np.percentile(err32, 99)),
                               "gpu_launches_per_step": launches32},
-                     "uneven_config3": dict(uneven, workload="131072 options, per-option x_dim in "
+                     "uneven_131072": dict(uneven, workload="131072 options, per-option x_dim in "
                                             "{128..2048} by vol*sqrt(T), t_dim=clamp(ceil(512 sqrt(T)),64,2048), "
                                             "uniform grids, scale 5; kwg_fd1d_price_uneven (host API, CUDA graph)"),
-                     "fd1d_bs_config2": fd1d_bs,
-                     "precision_config4": config4,
+                     "fd1d_bs_32768x1024": fd1d_bs,
+                     "precision_65536x2048": fine,
                      "autotune": tuned,
-                     "surrogate_config5": surrogate},
+                     "surrogate_1m": surrogate},
     }
     print(json.dumps(line), flush=True)
 
@@ -596,9 +596,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--ref-options", type=int, default=256, help="options per reference step")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch (config 3) variant")
-    ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate (config 5) variant")
-    ap.add_argument("--no-config4", action="store_true", help="skip the 2048x2048 precision study (config 4)")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch (131072 options) variant")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate (1M options) variant")
+    ap.add_argument("--no-fine-study", action="store_true", help="skip the 65536-option 2048x2048 precision study")
     ap.add_argument("--surrogate-options", type=int, default=SURROGATE_OPTIONS)
     ap.add_argument("--options", type=int, default=N_OPTIONS,
                     help="options per batch (default 32768; smaller values are for profiling captures)")

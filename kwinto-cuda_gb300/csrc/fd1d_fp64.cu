@@ -55,7 +55,7 @@ namespace {
 
 constexpr int kCoef = 3;                                   // coefficients per node and sweep
 constexpr int kConsts = 6;                                 // nh l 1/e uh m 1/d in the middle
-constexpr int kGroup = 4;                                  // nodes per stage
+constexpr int kGroup = 8;                                  // nodes per stage
 constexpr uint32_t kNodeCoefBytes = kCoef * kTile * 8;    // 768 B
 constexpr uint32_t kNodePBytes = kTile * 8;               // 256 B
 constexpr uint32_t kNodeSBytes = 2 * kTile * 8;           // 512 B
@@ -276,10 +276,14 @@ namespace {
 // sweep: coefficients [kGroup][3][32], payoff [kGroup][32], state [kGroup][32][2].
 // Stage visits are numbered per warp (q); visit q uses stage q % kRing with
 // mbarrier parity (q / kRing) & 1.
-constexpr int kRing = 4;
-constexpr uint32_t kStageCoef = kGroup * kNodeCoefBytes;  // 3 KB
-constexpr uint32_t kStageP = kGroup * kNodePBytes;        // 1 KB
-constexpr uint32_t kStageS = kGroup * kNodeSBytes;        // 2 KB
+// 8-node stages, double-buffered: 24 KB per warp keeps >= 7 single-warp blocks per
+// SM (the 1024 tiles of a 32768-option batch in one wave), and measured on the 32768-option
+// 1024 x 1024 batch (launch ms, nodes x ring): 4x4 246, 6x3 236, 7x2 223, 8x2 219, 10x2 401 (6 blocks
+// per SM: a second wave), 2x8 314
+constexpr int kRing = 2;
+constexpr uint32_t kStageCoef = kGroup * kNodeCoefBytes;  // 6 KB
+constexpr uint32_t kStageP = kGroup * kNodePBytes;        // 2 KB
+constexpr uint32_t kStageS = kGroup * kNodeSBytes;        // 4 KB
 constexpr uint32_t kStageBytes = kStageCoef + kStageP + kStageS;
 // one warp's ring and mbarriers, rounded so the next warp's stages stay aligned
 constexpr size_t kSolveSmem = (kRing * kStageBytes + kRing * sizeof(uint64_t) + 127) / 128 * 128;
@@ -392,6 +396,8 @@ __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileVi
                 rs[k] = compact ? cs : sc_[(idx * kCoef + 2) * kTile];
             }
         }
+        __syncwarp();  // stage s fully read before it is refilled
+        if (lane == 0 && g + kRing < ng) issue<kUp>(ring, v + kRing, tv, g + kRing, N, rg);
 #pragma unroll
         for (int k = 0; k < kGroup; ++k) {
             if (k < count) {
@@ -403,10 +409,6 @@ __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileVi
                 if (active) sout[(size_t)j * kTile] = make_double2(vn, f);
             }
         }
-        // refill after the stage's FMA chain is under way (the ring still runs three
-        // stages ahead); every lane read the stage into registers above
-        __syncwarp();
-        if (lane == 0 && g + kRing < ng) issue<kUp>(ring, v + kRing, tv, g + kRing, N, rg);
     }
     return true;
 }
@@ -416,8 +418,8 @@ __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileVi
 // Persistent: each warp takes tiles from tile_counter[0] (zeroed by the host before
 // the launch) and runs all tDim-1 steps of its 32 PDEs.  A block holds 1, 2 or 4
 // independent warps (32 options each; each warp has its own ring); the block size is
-// a tuned launch parameter.  The sweeps stream through a 4-deep
-// ring of 4-node stages in shared memory filled by the TMA engine; V and h|f are
+// a tuned launch parameter.  The sweeps stream through a 2-deep
+// ring of 8-node stages in shared memory filled by the TMA engine; V and h|f are
 // written back with ordinary 16-byte stores.  If a ring wait expires,
 // tile_counter[1] is set, the warp drains its copies in flight and leaves; the
 // interpolation kernel then marks every option with KWG_STATUS_DEVICE_TIMEOUT.

@@ -4,17 +4,18 @@ Random numbers: counter-based splitmix64.  Field f of option i takes the 64-bit
 output of splitmix64's finaliser applied to  seed*2^40 + f*2^32 + i + 1  times the
 golden-ratio increment, and the top 53 bits give a uniform double in [0, 1).  The
 same function is used by tests, the benchmark and the oracle runs, so every
-workload is reproducible from (config, seed, n).
+workload is reproducible from (workload, seed, n).
 
 Workloads (the shapes the reference logs use, log/*_1024_32768.log):
-  config1   128 American options, half puts half calls, S=100, K~U[80,120],
-            vol~U[0.1,0.6], r~U[0,0.1], q~U[0,0.1], T~U[0.25,2]; 512x512 grid,
-            scale 5, density 0.25 (the reference default)
-  config2   the same distributions, 32768 options, 1024x1024, uniform grid
-  config3   uneven batch: T log-uniform [1/52, 5], K/S lognormal(0, 0.2),
-            vol~U[0.05,0.8], r,q~U[0,0.08]; per-option x_dim by vol*sqrt(T) bucket,
-            t_dim = clamp(ceil(512 sqrt(T)), 64, 2048)
-  config4   config-1 distributions, 65536 options, 2048x2048
+  american_128x512     128 American options, half puts half calls, S=100,
+                       K~U[80,120], vol~U[0.1,0.6], r~U[0,0.1], q~U[0,0.1],
+                       T~U[0.25,2]; 512x512 grid, scale 5, density 0.25 (the
+                       reference default)
+  american_32768x1024  the same distributions, 32768 options, 1024x1024, uniform grid
+  american_65536x2048  the same distributions, 65536 options, 2048x2048
+  uneven_portfolio     131072 options: T log-uniform [1/52, 5], K/S lognormal(0, 0.2),
+                       vol~U[0.05,0.8], r,q~U[0,0.08]; per-option x_dim by vol*sqrt(T)
+                       bucket, t_dim = clamp(ceil(512 sqrt(T)), 64, 2048)
 """
 from __future__ import annotations
 
@@ -47,9 +48,9 @@ def _normals(seed: int, field: int, n: int, start: int = 0) -> np.ndarray:
     return np.sqrt(-2.0 * np.log1p(-u1)) * np.cos(2.0 * math.pi * u2)
 
 
-def config1_like(n: int, seed: int = 42, start: int = 0) -> np.ndarray:
-    """Config-1 distributions (also config 2 and 4): all American, puts on even
-    indices, calls on odd ones."""
+def american_portfolio(n: int, seed: int = 42, start: int = 0) -> np.ndarray:
+    """American options: S=100, K~U[80,120], vol~U[0.1,0.6], r,q~U[0,0.1],
+    T~U[0.25,2]; puts on even indices, calls on odd ones."""
     o = np.zeros(n, OPTION_DTYPE)
     o["s"] = 100.0
     o["k"] = 80.0 + 40.0 * uniforms(seed, 0, n, start)
@@ -63,10 +64,10 @@ def config1_like(n: int, seed: int = 42, start: int = 0) -> np.ndarray:
     return o
 
 
-CONFIGS = {
-    "config1": dict(n=128, x_dim=512, t_dim=512, scale=5.0, density=0.25),
-    "config2": dict(n=32768, x_dim=1024, t_dim=1024, scale=5.0, density=math.inf),
-    "config4": dict(n=65536, x_dim=2048, t_dim=2048, scale=5.0, density=0.25),
+WORKLOADS = {
+    "american_128x512": dict(n=128, x_dim=512, t_dim=512, scale=5.0, density=0.25),
+    "american_32768x1024": dict(n=32768, x_dim=1024, t_dim=1024, scale=5.0, density=math.inf),
+    "american_65536x2048": dict(n=65536, x_dim=2048, t_dim=2048, scale=5.0, density=0.25),
 }
 
 # The reference has no uniform-grid mode; its closest setting is a large density.
@@ -74,7 +75,7 @@ CONFIGS = {
 REFERENCE_UNIFORM_DENSITY = 1e6
 
 
-def config3(n: int = 131072, seed: int = 42, start: int = 0):
+def uneven_portfolio(n: int = 131072, seed: int = 42, start: int = 0):
     """Uneven batch.  Returns (options, x_dim[n], t_dim[n])."""
     o = np.zeros(n, OPTION_DTYPE)
     o["s"] = 100.0

@@ -20,12 +20,12 @@ def window(n_per_rank: int, rank: int) -> tuple[int, int]:
     return rank * n_per_rank, n_per_rank
 
 
-def config_shard(n_per_rank: int, rank: int, seed: int = 42) -> np.ndarray:
-    """Rank's options of the config-1/2/4 stream (weak scaling)."""
+def portfolio_shard(n_per_rank: int, rank: int, seed: int = 42) -> np.ndarray:
+    """Rank's window of the American-option stream (weak scaling)."""
     import portfolio
 
     start, n = window(n_per_rank, rank)
-    return portfolio.config1_like(n, seed=seed, start=start)
+    return portfolio.american_portfolio(n, seed=seed, start=start)
 
 
 def partition_by_work(x_dims, t_dims, world: int) -> list[tuple[int, int]]:

@@ -55,7 +55,7 @@ def evaluate(net: kwg.Surrogate, ctx, n: int, grid: int, seed: int = TEST_SEED) 
     """Network prices vs FD64 on n fresh options."""
     import torch
 
-    opts = portfolio.config1_like(n, seed=seed)
+    opts = portfolio.american_portfolio(n, seed=seed)
     d_o = torch.from_numpy(opts.view(np.uint8).copy()).cuda()
     fd = fd64_device(ctx, d_o, n, grid).cpu().numpy()
     d_p = torch.empty(n, dtype=torch.float64, device="cuda")
@@ -82,7 +82,7 @@ def main(argv=None):
     import torch
 
     ctx = kwg.Context(0)
-    opts = portfolio.config1_like(a.n, seed=TRAIN_SEED)
+    opts = portfolio.american_portfolio(a.n, seed=TRAIN_SEED)
     d_o = torch.from_numpy(opts.view(np.uint8).copy()).cuda()
     t0 = time.perf_counter()
     d_p = fd64_device(ctx, d_o, a.n, a.grid)

@@ -99,19 +99,19 @@ def main(ref: str):
         out[f"portfolio_{name}"] = dict(n=int(len(amer)), max_abs_vs_quantlib=float(np.max(np.abs(fd - qd))))
 
     # 3. Synthetic workloads at their grids (reference has no uniform mode: d = 1e6).
-    o1 = portfolio.config1_like(128, seed=42)
+    o1 = portfolio.american_portfolio(128, seed=42)
     rc, msg, p1 = ref_twice(o1, pricer="FD1D", density=0.25, scale=5.0, t_dim=512, x_dim=512)
     assert rc == 0, msg
-    o2 = portfolio.config1_like(256, seed=42)
+    o2 = portfolio.american_portfolio(256, seed=42)
     rc, msg, p2 = ref_twice(o2, pricer="FD1D", density=portfolio.REFERENCE_UNIFORM_DENSITY, scale=5.0,
                             t_dim=1024, x_dim=1024)
     assert rc == 0, msg
-    o4 = portfolio.config1_like(32, seed=42)
+    o4 = portfolio.american_portfolio(32, seed=42)
     rc, msg, p4 = ref_twice(o4, pricer="FD1D", density=0.25, scale=5.0, t_dim=2048, x_dim=2048)
     assert rc == 0, msg
-    np.savez_compressed(os.path.join(HERE, "synthetic.npz"), config1_opts=o1, config1_ref=p1,
-                        config2_opts=o2, config2_ref=p2, config4_opts=o4, config4_ref=p4)
-    out["synthetic"] = dict(config1=len(o1), config2_sample=len(o2), config4_sample=len(o4))
+    np.savez_compressed(os.path.join(HERE, "synthetic.npz"), small_opts=o1, small_ref=p1,
+                        batch1024_opts=o2, batch1024_ref=p2, fine2048_opts=o4, fine2048_ref=p4)
+    out["synthetic"] = dict(small=len(o1), batch1024_sample=len(o2), fine2048_sample=len(o4))
 
     # 4. Edge cases: European options, calls/puts, duplicates (dedup path), odd grids,
     #    and an out-of-grid spot (the reference fails the whole call).

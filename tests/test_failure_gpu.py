@@ -21,7 +21,7 @@ def test_bounded_wait_times_out_and_context_survives(ctx):
     import portfolio
 
     assert ctx.selftest_waits() == (1, 1)
-    o = portfolio.config1_like(64, seed=3)
+    o = portfolio.american_portfolio(64, seed=3)
     rc, p, st = ctx.fd1d_price(o, kwg.params(t_dim=64, x_dim=64, scale=5.0))
     assert rc == kwg.KWG_OK and (st == 0).all() and np.isfinite(p).all()
 
@@ -31,7 +31,7 @@ def test_degenerate_factorisation_is_a_per_option_status(ctx, precision, solver)
     import kwg
     import portfolio
 
-    o = portfolio.config1_like(100, seed=4)
+    o = portfolio.american_portfolio(100, seed=4)
     bad = o.copy()
     bad["z"][[7, 50]] = 1e200
     prm = kwg.params(t_dim=64, x_dim=128, scale=5.0, precision=precision, solver=solver)

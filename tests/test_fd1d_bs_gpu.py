@@ -40,13 +40,13 @@ def test_pricer_test_table(ctx, solver):
     assert np.max(np.abs(p - g["want"])) <= 1.3e-3
 
 
-def test_config1_vs_oracle(ctx):
+def test_128_options_vs_oracle(ctx):
     import kwor
 
     g = golden("synthetic.npz")
     kw = dict(t_dim=512, x_dim=512, scale=5.0, density=0.25)
-    p, st = bs_price(ctx, g["config1_opts"], **kw)
-    rc, msg, want, _ = kwor.fd1d_price(g["config1_opts"], bs=True, **kw)
+    p, st = bs_price(ctx, g["small_opts"], **kw)
+    rc, msg, want, _ = kwor.fd1d_price(g["small_opts"], bs=True, **kw)
     assert rc == 0, msg
     assert (st == 0).all()
     assert rel_err(p, want) <= REL_TOL
@@ -71,7 +71,7 @@ def test_european_assets_get_black_scholes(ctx):
     import kwor
     import portfolio
 
-    o = portfolio.config1_like(256, seed=8)
+    o = portfolio.american_portfolio(256, seed=8)
     o["e"] = 0
     p, st = bs_price(ctx, o, t_dim=256, x_dim=256, scale=5.0, density=math.inf)
     assert (st == 0).all()
@@ -83,7 +83,7 @@ def test_fp32_close_to_fp64(ctx):
     import kwg
     import portfolio
 
-    o = portfolio.config1_like(2048, seed=9)
+    o = portfolio.american_portfolio(2048, seed=9)
     kw = dict(t_dim=1024, x_dim=1024, scale=5.0, density=math.inf)
     p64, _ = bs_price(ctx, o, **kw)
     p32, st = bs_price(ctx, o, precision=kwg.FP32, **kw)

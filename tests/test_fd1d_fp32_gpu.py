@@ -28,25 +28,25 @@ def oracle(opts, **kw):
     return p
 
 
-def test_config1(ctx):
+def test_128_options_512_grid(ctx):
     g = golden("synthetic.npz")
-    p, st = price32(ctx, g["config1_opts"], t_dim=512, x_dim=512, scale=5.0, density=0.25)
+    p, st = price32(ctx, g["small_opts"], t_dim=512, x_dim=512, scale=5.0, density=0.25)
     assert (st == 0).all()
-    assert np.max(np.abs(p - g["config1_ref"])) <= ABS_TOL
+    assert np.max(np.abs(p - g["small_ref"])) <= ABS_TOL
 
 
-def test_config2_sample_uniform(ctx):
+def test_1024_grid_sample_uniform(ctx):
     g = golden("synthetic.npz")
-    p, st = price32(ctx, g["config2_opts"], t_dim=1024, x_dim=1024, scale=5.0, density=math.inf)
+    p, st = price32(ctx, g["batch1024_opts"], t_dim=1024, x_dim=1024, scale=5.0, density=math.inf)
     assert (st == 0).all()
-    assert np.max(np.abs(p - g["config2_ref"])) <= ABS_TOL
+    assert np.max(np.abs(p - g["batch1024_ref"])) <= ABS_TOL
 
 
-def test_config4_sample(ctx):
+def test_2048_grid_sample(ctx):
     g = golden("synthetic.npz")
-    p, st = price32(ctx, g["config4_opts"], t_dim=2048, x_dim=2048, scale=5.0, density=0.25)
+    p, st = price32(ctx, g["fine2048_opts"], t_dim=2048, x_dim=2048, scale=5.0, density=0.25)
     assert (st == 0).all()
-    assert np.max(np.abs(p - g["config4_ref"])) <= ABS_TOL
+    assert np.max(np.abs(p - g["fine2048_ref"])) <= ABS_TOL
 
 
 def test_portfolio_qdfp(ctx):
@@ -81,7 +81,7 @@ def test_non_power_of_two_grids(ctx, x_dim, t_dim):
     coefficients are built in FP64 for exactly this case."""
     import portfolio
 
-    o = portfolio.config1_like(40, seed=21)
+    o = portfolio.american_portfolio(40, seed=21)
     p, st = price32(ctx, o, t_dim=t_dim, x_dim=x_dim, scale=5.0, density=0.25)
     want = oracle(o, t_dim=t_dim, x_dim=x_dim, scale=5.0, density=0.25)
     assert (st == 0).all() and np.max(np.abs(p - want)) <= ABS_TOL
@@ -90,7 +90,7 @@ def test_non_power_of_two_grids(ctx, x_dim, t_dim):
 def test_theta_and_status(ctx):
     import kwg
 
-    o = golden("synthetic.npz")["config1_opts"][:24]
+    o = golden("synthetic.npz")["small_opts"][:24]
     p, _ = price32(ctx, o, t_dim=200, x_dim=256, scale=5.0, density=0.25, theta=1.0)
     want = oracle(o, t_dim=200, x_dim=256, scale=5.0, density=0.25, theta=1.0)
     assert np.max(np.abs(p - want)) <= ABS_TOL
@@ -101,12 +101,12 @@ def test_theta_and_status(ctx):
     assert rc == kwg.KWG_ERR_INVALID and "2048" in ctx.last_error()
 
 
-def test_config2_full_size_vs_fp64(ctx):
+def test_32768x1024_full_size_vs_fp64(ctx):
     """All 32768 options at 1024x1024: FP32 within 1e-5 of the GPU FP64 path."""
     import kwg
     import portfolio
 
-    o = portfolio.config1_like(32768, seed=42)
+    o = portfolio.american_portfolio(32768, seed=42)
     rc, p64, _ = ctx.fd1d_price(o, kwg.params(t_dim=1024, x_dim=1024, scale=5.0, density=math.inf))
     assert rc == 0
     p32, st = price32(ctx, o, t_dim=1024, x_dim=1024, scale=5.0, density=math.inf)

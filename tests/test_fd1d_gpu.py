@@ -54,26 +54,26 @@ def test_portfolio_fixtures(ctx, name, solver):
 
 
 @SOLVERS
-def test_config1(ctx, solver):
+def test_128_options_512_grid(ctx, solver):
     g = golden("synthetic.npz")
-    p, st = gpu_price(ctx, g["config1_opts"], t_dim=512, x_dim=512, scale=5.0, density=0.25, solver=solver)
-    assert (st == 0).all() and rel_err(p, g["config1_ref"]) <= REL_TOL
+    p, st = gpu_price(ctx, g["small_opts"], t_dim=512, x_dim=512, scale=5.0, density=0.25, solver=solver)
+    assert (st == 0).all() and rel_err(p, g["small_ref"]) <= REL_TOL
 
 
 @SOLVERS
-def test_config2_sample_sinh_and_uniform(ctx, solver):
+def test_1024_grid_sample_sinh_and_uniform(ctx, solver):
     """1024x1024: the reference at density 1e6, the GPU both at 1e6 and exactly uniform."""
     g = golden("synthetic.npz")
-    p, _ = gpu_price(ctx, g["config2_opts"], t_dim=1024, x_dim=1024, scale=5.0, density=1e6, solver=solver)
-    assert rel_err(p, g["config2_ref"]) <= REL_TOL
-    u, _ = gpu_price(ctx, g["config2_opts"], t_dim=1024, x_dim=1024, scale=5.0, density=math.inf, solver=solver)
-    assert rel_err(u, g["config2_ref"]) <= REL_TOL
+    p, _ = gpu_price(ctx, g["batch1024_opts"], t_dim=1024, x_dim=1024, scale=5.0, density=1e6, solver=solver)
+    assert rel_err(p, g["batch1024_ref"]) <= REL_TOL
+    u, _ = gpu_price(ctx, g["batch1024_opts"], t_dim=1024, x_dim=1024, scale=5.0, density=math.inf, solver=solver)
+    assert rel_err(u, g["batch1024_ref"]) <= REL_TOL
 
 
-def test_config4_sample(ctx):
+def test_2048_grid_sample(ctx):
     g = golden("synthetic.npz")
-    p, _ = gpu_price(ctx, g["config4_opts"], t_dim=2048, x_dim=2048, scale=5.0, density=0.25)
-    assert rel_err(p, g["config4_ref"]) <= REL_TOL
+    p, _ = gpu_price(ctx, g["fine2048_opts"], t_dim=2048, x_dim=2048, scale=5.0, density=0.25)
+    assert rel_err(p, g["fine2048_ref"]) <= REL_TOL
 
 
 @SOLVERS
@@ -104,7 +104,7 @@ def test_theta_other_than_half(ctx, theta, solver):
     """theta is hard-coded to 0.5 in the reference; other values follow the oracle."""
     import kwor
 
-    o = golden("synthetic.npz")["config1_opts"][:40]
+    o = golden("synthetic.npz")["small_opts"][:40]
     p, _ = gpu_price(ctx, o, t_dim=200, x_dim=160, scale=5.0, density=0.25, theta=theta, solver=solver)
     rc, msg, want, _ = kwor.fd1d_price(o, t_dim=200, x_dim=160, scale=5.0, density=0.25, theta=theta)
     assert rc == 0, msg
@@ -118,7 +118,7 @@ def test_ragged_batches(ctx, n, solver):
     import kwor
     import portfolio
 
-    o = portfolio.config1_like(n, seed=99)
+    o = portfolio.american_portfolio(n, seed=99)
     p, st = gpu_price(ctx, o, t_dim=64, x_dim=96, scale=5.0, density=0.25, solver=solver)
     rc, msg, want, _ = kwor.fd1d_price(o, t_dim=64, x_dim=96, scale=5.0, density=0.25)
     assert (st == 0).all() and rel_err(p, want) <= REL_TOL
@@ -157,7 +157,7 @@ def test_device_api_matches_host_api(ctx):
     import kwg
     import portfolio
 
-    o = portfolio.config1_like(300, seed=5)
+    o = portfolio.american_portfolio(300, seed=5)
     prm = kwg.params(t_dim=128, x_dim=256, scale=5.0, density=0.25)
     want, _ = gpu_price(ctx, o, t_dim=128, x_dim=256, scale=5.0, density=0.25)
     d_o = torch.from_numpy(o.view(np.uint8).copy()).cuda()
@@ -220,7 +220,7 @@ def test_pricer_mirror(built):
     assert err.startswith("Fd1dGpu_Pricer::price:") and "not in grid range" in err
 
 
-def test_config2_full_size_properties(ctx):
+def test_32768x1024_full_size_properties(ctx):
     """All 32768 options at 1024x1024: finite, American >= intrinsic up to the
     interpolation error of the payoff, deterministic, and a sample equal to the oracle.
     The projection floors every node but the last at the payoff; between nodes the
@@ -229,7 +229,7 @@ def test_config2_full_size_properties(ctx):
     import kwor
     import portfolio
 
-    o = portfolio.config1_like(32768, seed=42)
+    o = portfolio.american_portfolio(32768, seed=42)
     p, st = gpu_price(ctx, o, t_dim=1024, x_dim=1024, scale=5.0, density=math.inf)
     assert (st == 0).all() and np.isfinite(p).all()
     intrinsic = np.where(o["w"] < 0, np.maximum(o["k"] - o["s"], 0), np.maximum(o["s"] - o["k"], 0))
@@ -248,7 +248,7 @@ def test_solvers_agree_and_autotune(ctx):
     import kwg
     import portfolio
 
-    o = portfolio.config1_like(777, seed=17)
+    o = portfolio.american_portfolio(777, seed=17)
     kw = dict(t_dim=300, x_dim=256, scale=5.0, density=0.25)
     a, _ = gpu_price(ctx, o, solver=kwg.SOLVER_THOMAS, **kw)
     b, _ = gpu_price(ctx, o, solver=kwg.SOLVER_PCR, **kw)

@@ -87,11 +87,11 @@ def test_factory_errors():
 def test_portfolio_generator_is_deterministic_and_in_range():
     import portfolio
 
-    a = portfolio.config1_like(1000, seed=42)
-    b = portfolio.config1_like(1000, seed=42)
+    a = portfolio.american_portfolio(1000, seed=42)
+    b = portfolio.american_portfolio(1000, seed=42)
     assert a.tobytes() == b.tobytes()
     # a window of the stream equals the same slice of the full stream
-    c = portfolio.config1_like(100, seed=42, start=500)
+    c = portfolio.american_portfolio(100, seed=42, start=500)
     assert c.tobytes() == a[500:600].tobytes()
     assert (a["k"] >= 80).all() and (a["k"] < 120).all()
     assert (a["z"] >= 0.1).all() and (a["z"] < 0.6).all()
@@ -101,10 +101,10 @@ def test_portfolio_generator_is_deterministic_and_in_range():
     assert abs(u.mean() - 0.5) < 5e-3 and u.min() >= 0 and u.max() < 1
 
 
-def test_config3_buckets():
+def test_uneven_buckets():
     import portfolio
 
-    o, xd, td = portfolio.config3(20000, seed=42)
+    o, xd, td = portfolio.uneven_portfolio(20000, seed=42)
     assert set(np.unique(xd)) <= {128, 256, 512, 1024, 2048}
     assert td.min() >= 64 and td.max() <= 2048
     assert (o["t"] >= 1 / 52 - 1e-12).all() and (o["t"] <= 5 + 1e-12).all()

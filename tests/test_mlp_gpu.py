@@ -139,14 +139,14 @@ LABEL_GRID = dict(t_dim=256, x_dim=256, scale=5.0, density=math.inf)
 
 @pytest.fixture(scope="module")
 def trained(ctx, built):
-    """A surrogate trained on the GPU on FD64 prices of 16384 options (config-1
-    distributions, 256 x 256 uniform grid) generated by the GPU solver."""
+    """A surrogate trained on the GPU on FD64 prices of 16384 options (S=100,
+    K~U[80,120], vol~U[0.1,0.6], r,q~U[0,0.1], T~U[0.25,2]; 256 x 256 uniform grid) generated by the GPU solver."""
     import torch
 
     import kwg
     import portfolio
 
-    opts = portfolio.config1_like(16384, seed=101)
+    opts = portfolio.american_portfolio(16384, seed=101)
     prices = _fd_prices(ctx, opts, **LABEL_GRID)
     d_o = torch.from_numpy(opts.view(np.uint8).copy()).cuda()
     d_p = torch.from_numpy(prices).cuda()
@@ -197,7 +197,7 @@ def test_trained_network_beats_analytic_prices(trained, ctx):
     import portfolio
 
     s = trained[0]
-    test = portfolio.config1_like(4096, seed=202)
+    test = portfolio.american_portfolio(4096, seed=202)
     fd = _fd_prices(ctx, test, **LABEL_GRID)
     d_o = torch.from_numpy(test.view(np.uint8).copy()).cuda()
     d_p = torch.empty(len(test), dtype=torch.float64, device="cuda")
@@ -222,7 +222,7 @@ def test_featurize_matches_oracle(net):
     import portfolio
 
     net.set_params(mo.random_params(1), mo.BOX_LO, mo.BOX_HI, 1.0)
-    o = portfolio.config1_like(5000, seed=55)
+    o = portfolio.american_portfolio(5000, seed=55)
     o["k"][::7] *= 1.5       # log K/S above the box
     o["z"][3::11] = 2.0      # vol sqrt T above the box
     o["e"][5::13] = 0        # European
@@ -265,7 +265,7 @@ def test_surrogate_routes_and_audits(trained, ctx):
     import portfolio
 
     s = trained[0]
-    opts = portfolio.config1_like(3000, seed=303)
+    opts = portfolio.american_portfolio(3000, seed=303)
     opts["z"][::50] = 2.0  # vol sqrt(T) >= 1 is outside the box (and the spot stays on the FD grid)
     opts["e"][1::50] = 0
     oob = np.zeros(len(opts), bool)
@@ -308,7 +308,7 @@ def test_fused_price_matches_layer_path(net, n):
 
     y_scale = 250.0
     net.set_params(mo.random_params(21), mo.BOX_LO, mo.BOX_HI, y_scale)
-    o = portfolio.config1_like(n, seed=n)
+    o = portfolio.american_portfolio(n, seed=n)
     if n > 10:
         o["e"][3::10] = 0
     d_o = torch.from_numpy(o.view(np.uint8).copy()).cuda()
@@ -345,7 +345,7 @@ def test_committed_weights_meet_the_error_target(ctx, built):
     path = os.path.join(os.path.dirname(kwg.__file__), "surrogate_weights.npz")
     s = kwg.Surrogate(0)
     s.load(path)
-    o = portfolio.config1_like(8192, seed=31337)
+    o = portfolio.american_portfolio(8192, seed=31337)
     fd = _fd_prices(ctx, o, t_dim=1024, x_dim=1024, scale=5.0, density=math.inf)
     d_o = torch.from_numpy(o.view(np.uint8).copy()).cuda()
     d_p = torch.empty(len(o), dtype=torch.float64, device="cuda")

@@ -87,7 +87,7 @@ def test_baw_published_calls():
 def test_baw_bounds_and_limits():
     import portfolio
 
-    o = portfolio.config1_like(4000, seed=9)
+    o = portfolio.american_portfolio(4000, seed=9)
     b, e = mo.baw(o), mo.european(o)
     intr = np.maximum(0, np.where(o["w"] < 0, o["k"] - o["s"], o["s"] - o["k"]))
     assert np.all(b >= e) and np.all(b >= intr - 1e-12 * o["k"])

@@ -33,7 +33,7 @@ def _rank_main(rank: int, world: int, port: int, out):
 
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
-        opts = shard.config_shard(N_PER_RANK, rank)
+        opts = shard.portfolio_shard(N_PER_RANK, rank)
         rc, msg, prices, status = kwor.fd1d_price(opts, nthreads=1, **GRID)
         slowest = shard.max_over_ranks(1.5 + rank)
         gathered = [None] * world
@@ -61,7 +61,7 @@ def test_two_gloo_ranks_shard_the_stream():
     # the timing reduction is the max over ranks
     assert slowest == 1.5 + (world - 1)
     # the shards are the consecutive windows of the single-process stream ...
-    whole = portfolio.config1_like(world * N_PER_RANK, seed=42)
+    whole = portfolio.american_portfolio(world * N_PER_RANK, seed=42)
     import kwg
 
     got = np.concatenate([np.frombuffer(g[0], dtype=kwg.OPTION_DTYPE) for g in gathered])
@@ -84,7 +84,7 @@ def test_partition_by_work_is_contiguous_and_balanced(world):
     import portfolio
     import shard
 
-    _, xd, td = portfolio.config3(4096, seed=5)
+    _, xd, td = portfolio.uneven_portfolio(4096, seed=5)
     chunks = shard.partition_by_work(xd, td, world)
     assert len(chunks) == world and chunks[0][0] == 0 and chunks[-1][1] == len(xd)
     assert all(chunks[r][1] == chunks[r + 1][0] for r in range(world - 1))

@@ -54,12 +54,12 @@ def test_portfolio_fixtures(kwor, name):
 
 def test_synthetic_workloads(kwor):
     g = golden("synthetic.npz")
-    rc, msg, p, _ = kwor.fd1d_price(g["config1_opts"], t_dim=512, x_dim=512, scale=5.0, density=0.25)
-    assert rc == 0 and np.array_equal(p, g["config1_ref"])
-    rc, msg, p, _ = kwor.fd1d_price(g["config2_opts"][:64], t_dim=1024, x_dim=1024, scale=5.0, density=1e6)
-    assert rc == 0 and np.array_equal(p, g["config2_ref"][:64])
-    rc, msg, p, _ = kwor.fd1d_price(g["config4_opts"][:4], t_dim=2048, x_dim=2048, scale=5.0, density=0.25)
-    assert rc == 0 and np.array_equal(p, g["config4_ref"][:4])
+    rc, msg, p, _ = kwor.fd1d_price(g["small_opts"], t_dim=512, x_dim=512, scale=5.0, density=0.25)
+    assert rc == 0 and np.array_equal(p, g["small_ref"])
+    rc, msg, p, _ = kwor.fd1d_price(g["batch1024_opts"][:64], t_dim=1024, x_dim=1024, scale=5.0, density=1e6)
+    assert rc == 0 and np.array_equal(p, g["batch1024_ref"][:64])
+    rc, msg, p, _ = kwor.fd1d_price(g["fine2048_opts"][:4], t_dim=2048, x_dim=2048, scale=5.0, density=0.25)
+    assert rc == 0 and np.array_equal(p, g["fine2048_ref"][:4])
 
 
 def test_edge_cases(kwor):
@@ -89,11 +89,11 @@ def test_const_dt_and_uniform_are_close(kwor):
     """The GPU uses dt = T/(tDim-1) on every step and an exactly uniform grid for
     density=inf; both stay far inside the 1e-10 parity bar."""
     g = golden("synthetic.npz")
-    o = g["config1_opts"][:32]
+    o = g["small_opts"][:32]
     _, _, a, _ = kwor.fd1d_price(o, t_dim=512, x_dim=512, scale=5.0, density=0.25)
     _, _, b, _ = kwor.fd1d_price(o, t_dim=512, x_dim=512, scale=5.0, density=0.25, const_dt=True)
     assert np.max(np.abs(a - b) / a) < 1e-11
-    o2 = g["config2_opts"][:16]
+    o2 = g["batch1024_opts"][:16]
     _, _, c, _ = kwor.fd1d_price(o2, t_dim=256, x_dim=256, scale=5.0, density=1e6)
     _, _, d, _ = kwor.fd1d_price(o2, t_dim=256, x_dim=256, scale=5.0, density=float("inf"))
     assert np.max(np.abs(c - d) / c) < 1e-10
@@ -112,7 +112,7 @@ def test_reference_matches_oracle_live(kwor):
         pytest.skip("reference library not built here")
     import portfolio
 
-    o = portfolio.config1_like(48, seed=1234)
+    o = portfolio.american_portfolio(48, seed=1234)
     runs = [kwor.ref_price(o, density=0.25, scale=5.0, t_dim=200, x_dim=300) for _ in range(2)]
     if not np.array_equal(runs[0][2], runs[1][2]):
         # the reference pool's wait() can return before the last job ends

@@ -23,7 +23,7 @@ def price(ctx, o, **kw):
 def test_block_warps_are_bit_identical(ctx, bw):
     import portfolio
 
-    o = portfolio.config1_like(3000, seed=17)  # 94 tiles: blocks with fewer warps than tiles at the tail
+    o = portfolio.american_portfolio(3000, seed=17)  # 94 tiles: blocks with fewer warps than tiles at the tail
     kw = dict(t_dim=96, x_dim=320, scale=5.0, density=0.25, solver=1)
     assert np.array_equal(price(ctx, o, block_warps=bw, **kw), price(ctx, o, block_warps=1, **kw))
 
@@ -37,7 +37,7 @@ def test_fp32_two_warps_per_option(ctx, x_dim):
     import kwor
     import portfolio
 
-    o = portfolio.config1_like(96, seed=x_dim)
+    o = portfolio.american_portfolio(96, seed=x_dim)
     dens = 0.25 if x_dim == 1000 else math.inf
     kw = dict(t_dim=128, x_dim=x_dim, scale=5.0, density=dens)
     p2 = price(ctx, o, precision=kwg.FP32, option_warps=2, **kw)
@@ -58,7 +58,7 @@ def test_autotune_records_and_applies_the_choice(ctx):
     best = min(timed)
     chosen = d["pcr_ms"] if d["solver"] == "pcr" else d["thomas_ms_by_block_warps"][d["block_warps"]]
     assert chosen == best
-    o = portfolio.config1_like(4096, seed=2)
+    o = portfolio.american_portfolio(4096, seed=2)
     auto = price(ctx, o, t_dim=64, x_dim=256, scale=5.0, density=math.inf)
     explicit = price(ctx, o, t_dim=64, x_dim=256, scale=5.0, density=math.inf, solver=t.solver,
                      block_warps=t.block_warps)
@@ -72,7 +72,7 @@ def test_autotune_uneven(ctx):
     import kwg
     import portfolio
 
-    o, xd, td = portfolio.config3(3000, seed=9)
+    o, xd, td = portfolio.uneven_portfolio(3000, seed=9)
     xd = np.minimum(xd, 1024)
     td = np.minimum(td, 200)
     prm = kwg.params(scale=5.0, density=math.inf)

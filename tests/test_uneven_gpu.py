@@ -1,4 +1,4 @@
-"""Uneven batches (config-3 shapes): every option on its own grid, one device pass.
+"""Uneven batches (per-option shapes): every option on its own grid, one device pass.
 The oracle -- like the reference, one grid shape per call -- is run per (x_dim,
 t_dim) group.  FP64 within REL_TOL = 1e-10 relative, FP32 within ABS_TOL = 1e-5."""
 import math
@@ -30,8 +30,8 @@ def oracle_uneven(opts, xd, td, density=math.inf):
 def sample(n, seed=42):
     import portfolio
 
-    o, xd, td = portfolio.config3(131072, seed=seed)
-    # a spread of shapes: evenly spaced options of the full config-3 stream
+    o, xd, td = portfolio.uneven_portfolio(131072, seed=seed)
+    # a spread of shapes: evenly spaced options of the full 131072-option uneven stream
     idx = np.linspace(0, 131071, n).astype(int)
     return o[idx], xd[idx], td[idx]
 
@@ -71,7 +71,7 @@ def test_uneven_uniform_shapes_match_uniform_call(ctx):
     import kwg
     import portfolio
 
-    o = portfolio.config1_like(100, seed=3)
+    o = portfolio.american_portfolio(100, seed=3)
     prm = kwg.params(t_dim=130, x_dim=256, scale=SCALE, density=math.inf, solver=1)
     rc, a, _ = ctx.fd1d_price(o, prm)
     assert rc == 0
@@ -115,12 +115,12 @@ def test_uneven_rejects_bad_shapes(ctx):
     assert rc == kwg.KWG_ERR_INVALID and "option 3" in ctx.last_error()
 
 
-def test_config3_full_size(ctx):
+def test_uneven_131072_full_size(ctx):
     """All 131072 options: statuses match the grid bounds, a sample matches the oracle."""
     import kwg
     import portfolio
 
-    o, xd, td = portfolio.config3(131072)
+    o, xd, td = portfolio.uneven_portfolio(131072)
     rc, p, st = ctx.fd1d_price_uneven(o, xd, td, kwg.params(scale=SCALE, density=math.inf))
     assert rc == 0, ctx.last_error()
     out = np.abs(np.log(o["s"] / o["k"])) >= 5 * o["z"] * np.sqrt(o["t"]) * (1 - 1e-9)

@@ -48,8 +48,8 @@ def test_static_scratch_matches_allocating_call(ctx):
     fn = _static_fn()
     stream = torch.cuda.Stream()
     err = ctypes.create_string_buffer(256)
-    cases = [(portfolio.config1_like(700, seed=11), kwg.params(t_dim=300, x_dim=1024, scale=5.0, density=0.25)),
-             (portfolio.config1_like(97, seed=12), kwg.params(t_dim=129, x_dim=257, scale=5.0, density=np.inf))]
+    cases = [(portfolio.american_portfolio(700, seed=11), kwg.params(t_dim=300, x_dim=1024, scale=5.0, density=0.25)),
+             (portfolio.american_portfolio(97, seed=12), kwg.params(t_dim=129, x_dim=257, scale=5.0, density=np.inf))]
     for opts, prm in cases:
         d_o, d_p, d_s = _device_batch(opts)
         rc = fn(d_o.data_ptr(), len(opts), ctypes.byref(prm), d_p.data_ptr(), d_s.data_ptr(), stream.cuda_stream,
@@ -74,7 +74,7 @@ def test_static_scratch_rejects_oversized_batches(ctx):
 
     fn = _static_fn()
     err = ctypes.create_string_buffer(256)
-    opts = portfolio.config1_like(4096, seed=3)  # 4096 x 1024 nodes needs ~336 MB > 64 MiB
+    opts = portfolio.american_portfolio(4096, seed=3)  # 4096 x 1024 nodes needs ~336 MB > 64 MiB
     prm = kwg.params(t_dim=16, x_dim=1024)
     d_o, d_p, d_s = _device_batch(opts)
     rc = fn(d_o.data_ptr(), len(opts), ctypes.byref(prm), d_p.data_ptr(), d_s.data_ptr(), None, err, 256)
