@@ -259,3 +259,49 @@ def test_solvers_agree_and_autotune(ctx):
     assert rel_err(c, a) <= REL_TOL
     t_ms, p_ms = ctx.autotune(kwg.params(t_dim=64, x_dim=2048, scale=5.0), 64)
     assert t_ms > 0 and p_ms < 0  # PCR-FP64 stops at x_dim 1024
+
+
+def test_large_grid_beyond_the_on_chip_limits(ctx):
+    """The streaming FP64 solver has no grid-size cap: 4096 nodes x 300 time levels
+    (twice the largest on-chip grid) against the oracle, puts and calls, sinh grid."""
+    import kwor
+    import portfolio
+
+    o = portfolio.american_portfolio(12, seed=4096)
+    kw = dict(t_dim=300, x_dim=4096, scale=5.0, density=0.25)
+    p, st = gpu_price(ctx, o, solver=1, **kw)
+    rc, msg, want, _ = kwor.fd1d_price(o, **kw)
+    assert rc == 0, msg
+    assert (st == 0).all() and rel_err(p, want) <= REL_TOL
+
+
+@pytest.mark.parametrize("entry", ["host", "bs", "device", "device_dedup", "uneven"])
+def test_single_option(ctx, entry):
+    """n = 1 through every entry point (one partly filled tile / warp)."""
+    import torch
+
+    import kwg
+    import kwor
+    import portfolio
+
+    o = portfolio.american_portfolio(1, seed=1)
+    prm = kwg.params(t_dim=64, x_dim=96, scale=5.0, density=0.25)
+    rc, msg, want, _ = kwor.fd1d_price(o, bs=(entry == "bs"), t_dim=64, x_dim=96, scale=5.0, density=0.25)
+    assert rc == 0, msg
+    if entry == "host":
+        rc, p, st = ctx.fd1d_price(o, prm)
+    elif entry == "bs":
+        rc, p, st = ctx.fd1d_bs_price(o, prm)
+    elif entry == "uneven":
+        rc, p, st = ctx.fd1d_price_uneven(o, [96], [64], prm)
+    else:
+        prm.device_dedup = 1 if entry == "device_dedup" else 0
+        d_o = torch.from_numpy(o.view(np.uint8).copy()).cuda()
+        d_p = torch.empty(1, dtype=torch.float64, device="cuda")
+        d_s = torch.empty(1, dtype=torch.int32, device="cuda")
+        rc = ctx.fd1d_price_device(d_o.data_ptr(), 1, prm, d_p.data_ptr(), d_s.data_ptr(),
+                                   torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        p, st = d_p.cpu().numpy(), d_s.cpu().numpy()
+    assert rc == 0 and st[0] == 0
+    assert rel_err(p, want) <= REL_TOL
