@@ -482,6 +482,9 @@ def run_ours(args):
     if not args.no_fine_study:
         o4 = portfolio.american_portfolio(65536, seed=44, start=rank * 65536)
         res4 = {}
+        # threads per option of the FP32 solver on this shape (2 or 4 warps at 2048 nodes)
+        tune4 = ctx.autotune_ex(kwg.params(t_dim=2048, x_dim=2048, scale=SCALE, density=0.25, precision=kwg.FP32),
+                                len(o4)).as_dict()
         for name, prec in (("fp64", kwg.FP64), ("fp32", kwg.FP32)):
             p4 = kwg.params(t_dim=2048, x_dim=2048, scale=SCALE, density=0.25, precision=prec)
             rc, pr4, st4 = ctx.fd1d_price(o4, p4)  # warm-up (allocations)
@@ -504,7 +507,9 @@ def run_ours(args):
                    "fd32_p99_abs_err_vs_fd64": float(np.percentile(e_abs, 99)),
                    "fd32_max_rel_err_vs_fd64": float(e_rel.max()),
                    "fd32_p99_rel_err_vs_fd64": float(np.percentile(e_rel, 99)),
-                   "failed": int((~ok4).sum())}
+                   "failed": int((~ok4).sum()),
+                   "fp32_tuning": {"option_warps": tune4["option_warps"],
+                                   "fp32_ms_by_option_warps": tune4["fp32_ms_by_option_warps"]}}
         if not args.no_cpu and rank == 0:
             sys.path.insert(0, os.path.join(ROOT, "oracle"))
             import kwor

@@ -83,8 +83,8 @@ typedef struct kwg_fd1d_params {
     int32_t block_warps;  /* FP64 streaming solver: warps (32 options each) per thread
                              block, 1, 2 or 4; 0 (default) = tuned or 1 */
     int32_t option_warps; /* warp-per-PDE FP32 solver: warps (32 threads each) per
-                             option, 1 or 2 (grids of more than 1024 nodes always 2);
-                             0 (default) = tuned or 1 */
+                             option, 1, 2 or 4 (grids of more than 1024 nodes at least
+                             2; at least 2 nodes per lane); 0 (default) = tuned or 1 */
 } kwg_fd1d_params;
 
 typedef struct kwg_ctx kwg_ctx;
@@ -166,12 +166,14 @@ typedef struct kwg_tuning {
     int32_t reserved;
     double thomas_ms[3];  /* streaming FP64 solver with 1, 2, 4 warps per block */
     double pcr_ms;        /* FP64 warp-per-PDE solver */
-    double fp32_ms[2];    /* FP32 solver with 1, 2 warps per option */
+    double fp32_ms[3];    /* FP32 solver with 1, 2, 4 warps per option (the launch may
+                             use fewer: at least 2 nodes per lane, and at least 2 warps
+                             for grids of more than 1024 nodes) */
 } kwg_tuning;
 
 /* Autotuner (no counterpart in the reference): on a synthetic batch of m options of
  * p's shape and precision, times options-per-block (1, 2, 4 warps of 32 per block)
- * and Thomas vs PCR for FP64, threads-per-option (1 or 2 warps) for FP32, and records
+ * and Thomas vs PCR for FP64, threads-per-option (1, 2 or 4 warps) for FP32, and records
  * the fastest for later calls of that shape whose p leaves the choices at 0 / AUTO.
  * `out` may be NULL. */
 int kwg_autotune_ex(kwg_ctx* ctx, const kwg_fd1d_params* p, size_t m, kwg_tuning* out);

@@ -584,6 +584,10 @@ void fd1d_fp32_prepare(int)
     prepare_m<8, 2>();
     prepare_m<16, 2>();
     prepare_m<32, 2>();
+    prepare_m<2, 4>();
+    prepare_m<4, 4>();
+    prepare_m<8, 4>();
+    prepare_m<16, 4>();
 }
 
 int fd1d_fp32_nodes_per_lane(int x_dim)
@@ -601,24 +605,33 @@ int fd1d_fp32_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh
 {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    // one warp per PDE (M = nodes per lane of a 32-lane layout) or, when asked and the
-    // grid has at least 4 nodes per lane, two warps of M/2 nodes per lane; grids of
-    // 1025..2048 nodes always take two warps of 32 nodes per lane
+    // W = 1, 2 or 4 warps per PDE (sh.option_warps), each lane owning M = m1 / W nodes,
+    // m1 the nodes per lane of the one-warp layout; at least 2 nodes per lane, and
+    // grids of 1025..2048 nodes take at least two warps
     const int m1 = fd1d_fp32_nodes_per_lane(sh.x_dim);
-    const bool two = m1 == 64 || (sh.option_warps == 2 && m1 >= 4);
-    switch (two ? m1 / 2 : m1) {
-    case 2: return two ? launch_m<2, 2>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev)
-                       : launch_m<2, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
-    case 4: return two ? launch_m<4, 2>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev)
-                       : launch_m<4, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
-    case 8: return two ? launch_m<8, 2>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev)
-                       : launch_m<8, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
-    case 16: return two ? launch_m<16, 2>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev)
-                        : launch_m<16, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
-    case 32: return two ? launch_m<32, 2>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev)
-                        : launch_m<32, 1>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
-    default: return -1;
-    }
+    if (m1 < 0) return -1;
+    int w = sh.option_warps == 4 ? 4 : sh.option_warps == 2 ? 2 : 1;
+    if (m1 == 64 && w < 2) w = 2;
+    while (w > 1 && m1 / w < 2) w /= 2;
+    const int M = m1 / w;
+#define KWG_FP32_LAUNCH(MM, WW) \
+    if (M == MM && w == WW) return launch_m<MM, WW>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev)
+    KWG_FP32_LAUNCH(2, 1);
+    KWG_FP32_LAUNCH(4, 1);
+    KWG_FP32_LAUNCH(8, 1);
+    KWG_FP32_LAUNCH(16, 1);
+    KWG_FP32_LAUNCH(32, 1);
+    KWG_FP32_LAUNCH(2, 2);
+    KWG_FP32_LAUNCH(4, 2);
+    KWG_FP32_LAUNCH(8, 2);
+    KWG_FP32_LAUNCH(16, 2);
+    KWG_FP32_LAUNCH(32, 2);
+    KWG_FP32_LAUNCH(2, 4);
+    KWG_FP32_LAUNCH(4, 4);
+    KWG_FP32_LAUNCH(8, 4);
+    KWG_FP32_LAUNCH(16, 4);
+#undef KWG_FP32_LAUNCH
+    return -1;
 }
 
 }  // namespace kwg

@@ -129,8 +129,8 @@ inline int check_params(kwg_ctx* ctx, const kwg_fd1d_params* p)
         return set_err(ctx, KWG_ERR_INVALID, "kwg: FP32 stepping supports x_dim <= 2048");
     if (p->block_warps != 0 && p->block_warps != 1 && p->block_warps != 2 && p->block_warps != 4)
         return set_err(ctx, KWG_ERR_INVALID, "kwg: block_warps must be 0, 1, 2 or 4");
-    if (p->option_warps < 0 || p->option_warps > 2)
-        return set_err(ctx, KWG_ERR_INVALID, "kwg: option_warps must be 0, 1 or 2");
+    if (p->option_warps != 0 && p->option_warps != 1 && p->option_warps != 2 && p->option_warps != 4)
+        return set_err(ctx, KWG_ERR_INVALID, "kwg: option_warps must be 0, 1, 2 or 4");
     return KWG_OK;
 }
 
@@ -168,7 +168,7 @@ inline kwg_ctx::Tuned tune(kwg_ctx* ctx, const kwg_fd1d_params* p, bool pcr_ok, 
     kwg_tuning r = {};
     for (double& v : r.thomas_ms) v = -1.;
     r.pcr_ms = -1.;
-    r.fp32_ms[0] = r.fp32_ms[1] = -1.;
+    for (double& v : r.fp32_ms) v = -1.;
     kwg_fd1d_params q = *p;
     q.strict = 0;
     kwg_ctx::Tuned best;
@@ -196,10 +196,11 @@ inline kwg_ctx::Tuned tune(kwg_ctx* ctx, const kwg_fd1d_params* p, bool pcr_ok, 
             consider(r.pcr_ms, KWG_SOLVER_PCR, 1, 1);
         }
     } else {
-        for (int w = 1; w <= 2; ++w) {
-            q.option_warps = w;
-            r.fp32_ms[w - 1] = time_solve(ctx, [&] { return fn(q); });
-            consider(r.fp32_ms[w - 1], KWG_SOLVER_PCR, 1, w);
+        const int ws[3] = {1, 2, 4};
+        for (int i = 0; i < 3; ++i) {
+            q.option_warps = ws[i];
+            r.fp32_ms[i] = time_solve(ctx, [&] { return fn(q); });
+            consider(r.fp32_ms[i], KWG_SOLVER_PCR, 1, ws[i]);
         }
     }
     r.solver = best.solver;

@@ -83,14 +83,15 @@ class Tuning(ctypes.Structure):
         ("reserved", ctypes.c_int32),
         ("thomas_ms", ctypes.c_double * 3),
         ("pcr_ms", ctypes.c_double),
-        ("fp32_ms", ctypes.c_double * 2),
+        ("fp32_ms", ctypes.c_double * 3),
     ]
 
     def as_dict(self) -> dict:
         return {"solver": {SOLVER_THOMAS: "thomas", SOLVER_PCR: "pcr"}.get(self.solver, self.solver),
                 "block_warps": self.block_warps, "option_warps": self.option_warps,
                 "thomas_ms_by_block_warps": {1: self.thomas_ms[0], 2: self.thomas_ms[1], 4: self.thomas_ms[2]},
-                "pcr_ms": self.pcr_ms, "fp32_ms_by_option_warps": {1: self.fp32_ms[0], 2: self.fp32_ms[1]}}
+                "pcr_ms": self.pcr_ms,
+                "fp32_ms_by_option_warps": {1: self.fp32_ms[0], 2: self.fp32_ms[1], 4: self.fp32_ms[2]}}
 
 
 _lib = None
