@@ -85,6 +85,11 @@ typedef struct kwg_fd1d_params {
     int32_t option_warps; /* warp-per-PDE FP32 solver: warps (32 threads each) per
                              option, 1, 2 or 4 (grids of more than 1024 nodes at least
                              2; at least 2 nodes per lane); 0 (default) = tuned or 1 */
+    int32_t sm_blocks;    /* FP64 streaming solver: resident blocks per SM, 0 (default) =
+                             tuned or as many as fit (two 4-warp blocks).  With
+                             block_warps 4 and sm_blocks 1 each of an SM's four warp
+                             schedulers runs one tile, whose FP64 pipe it then has to
+                             itself: it shortens the longest tiles of an uneven batch */
 } kwg_fd1d_params;
 
 typedef struct kwg_ctx kwg_ctx;
@@ -163,17 +168,18 @@ typedef struct kwg_tuning {
     int32_t solver;       /* KWG_SOLVER_THOMAS or KWG_SOLVER_PCR (FP64); KWG_SOLVER_PCR (FP32) */
     int32_t block_warps;  /* warps (32 options each) per block of the streaming FP64 solver */
     int32_t option_warps; /* warps (32 threads each) per option of the FP32 solver */
-    int32_t reserved;
+    int32_t sm_blocks;    /* resident blocks per SM of the streaming FP64 solver (0: as many as fit) */
     double thomas_ms[3];  /* streaming FP64 solver with 1, 2, 4 warps per block */
     double pcr_ms;        /* FP64 warp-per-PDE solver */
     double fp32_ms[3];    /* FP32 solver with 1, 2, 4 warps per option (the launch may
                              use fewer: at least 2 nodes per lane, and at least 2 warps
                              for grids of more than 1024 nodes) */
+    double spread_ms;     /* streaming FP64 solver, 4 warps per block, one block per SM */
 } kwg_tuning;
 
 /* Autotuner (no counterpart in the reference): on a synthetic batch of m options of
- * p's shape and precision, times options-per-block (1, 2, 4 warps of 32 per block)
- * and Thomas vs PCR for FP64, threads-per-option (1, 2 or 4 warps) for FP32, and records
+ * p's shape and precision, times options-per-block (1, 2, 4 warps of 32 per block, and
+ * one 4-warp block per SM) and Thomas vs PCR for FP64, threads-per-option (1, 2 or 4 warps) for FP32, and records
  * the fastest for later calls of that shape whose p leaves the choices at 0 / AUTO.
  * `out` may be NULL. */
 int kwg_autotune_ex(kwg_ctx* ctx, const kwg_fd1d_params* p, size_t m, kwg_tuning* out);

@@ -546,7 +546,7 @@ __global__ void fd1d_interp_fp64(const PdeBatch b, const AssetBatch a, Fd1dShape
     if (status) status[i] = st;
 }
 
-int fd1d_fp64_solve_blocks(int ntiles, int device, int block_warps)
+int fd1d_fp64_solve_blocks(int ntiles, int device, int block_warps, int sm_blocks)
 {
     // occupancy per block size (1, 2, 4 warps), cached for one device
     static int cached_dev = -1, cached_sms = 0, cached_max[kMaxBlockWarps + 1] = {};
@@ -565,7 +565,8 @@ int fd1d_fp64_solve_blocks(int ntiles, int device, int block_warps)
     }
     const int bw = block_warps == 2 || block_warps == 4 ? block_warps : 1;
     const int want = (ntiles + bw - 1) / bw;  // one tile per warp at most
-    const int cap = cached_sms * cached_max[bw];
+    const int per_sm = sm_blocks > 0 && sm_blocks < cached_max[bw] ? sm_blocks : cached_max[bw];
+    const int cap = cached_sms * per_sm;
     return want < cap ? (want > 0 ? want : 1) : cap;
 }
 

@@ -62,6 +62,7 @@ struct Fd1dShape {
     // 32 options each) and warps per option of the FP32 solver (1, 2)
     int block_warps = 1;
     int option_warps = 1;
+    int sm_blocks = 0;  // FP64 streaming solver: resident blocks per SM (0: as many as fit)
 };
 
 __host__ __device__ inline int shape_x(const Fd1dShape& sh, int pde) { return sh.pde_x ? sh.pde_x[pde] : sh.x_dim; }
@@ -118,6 +119,6 @@ void fd1d_pcr64_prepare(int device);
 
 // Occupancy-derived persistent grid size (blocks of block_warps warps) for the FP64
 // solve kernel.
-int fd1d_fp64_solve_blocks(int ntiles, int device, int block_warps = 1);
+int fd1d_fp64_solve_blocks(int ntiles, int device, int block_warps = 1, int sm_blocks = 0);
 
 }  // namespace kwg

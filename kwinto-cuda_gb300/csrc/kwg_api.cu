@@ -253,7 +253,12 @@ kwg_ctx::Tuned choose(kwg_ctx* ctx, const kwg_fd1d_params* p, int m)
     }
     if (p->precision == KWG_FP32) t.solver = KWG_SOLVER_PCR;
     else if (p->solver != KWG_SOLVER_AUTO) t.solver = p->solver;
-    if (p->block_warps) t.block_warps = p->block_warps;
+    // an explicit block size or residency replaces the recorded pair (the tuner timed
+    // every block size at full residency)
+    if (p->block_warps || p->sm_blocks) {
+        if (p->block_warps) t.block_warps = p->block_warps;
+        t.sm_blocks = p->sm_blocks;
+    }
     if (p->option_warps) t.option_warps = p->option_warps;
     return t;
 }
@@ -281,6 +286,7 @@ int run_batch(kwg_ctx* ctx, char* io, const IoLayout& L, int m, int n, const kwg
     const int solver = tn.solver;
     sh.block_warps = tn.block_warps;
     sh.option_warps = tn.option_warps;
+    sh.sm_blocks = tn.sm_blocks;
     if (p->precision == KWG_FP64 && solver == KWG_SOLVER_PCR) {
         const size_t wbytes = kwg::fd1d_fp32_work_bytes(m, sh.x_dim);
         if (int rc = ensure_device(ctx, &ctx->d_work, &ctx->work_bytes, wbytes)) return rc;
@@ -300,7 +306,7 @@ int run_batch(kwg_ctx* ctx, char* io, const IoLayout& L, int m, int n, const kwg
     } else {
         const size_t wbytes = kwg::fd1d_fp64_work_bytes(m_pad, sh.x_dim);
         if (int rc = ensure_device(ctx, &ctx->d_work, &ctx->work_bytes, wbytes)) return rc;
-        const int blocks = kwg::fd1d_fp64_solve_blocks(m_pad / kwg::kTile, ctx->device, sh.block_warps);
+        const int blocks = kwg::fd1d_fp64_solve_blocks(m_pad / kwg::kTile, ctx->device, sh.block_warps, sh.sm_blocks);
         ctx->launches += kwg::fd1d_fp64_launch(b, a, sh, (double*)ctx->d_work, (int32_t*)(io + L.pde_status),
                                                ctx->d_counter, prices, status, blocks, stream, ctx->next_events());
     }
@@ -505,6 +511,7 @@ void kwg_fd1d_params_default(kwg_fd1d_params* p)
     p->strict = 0;
     p->device_dedup = 0;
     p->block_warps = 0;
+    p->sm_blocks = 0;
     p->option_warps = 0;
 }
 

@@ -35,11 +35,13 @@ struct kwg_ctx {
     uint64_t graph_sig = 0;
     int graph_launches = 0;
     // autotuner decisions: shape key -> solver (KWG_SOLVER_THOMAS or KWG_SOLVER_PCR),
-    // warps per block of the streaming solver, warps per option of the FP32 solver
+    // warps per block and resident blocks per SM (0: as many as fit) of the streaming
+    // solver, warps per option of the FP32 solver
     struct Tuned {
         int solver = KWG_SOLVER_THOMAS;
         int block_warps = 1;
         int option_warps = 1;
+        int sm_blocks = 0;
     };
     std::map<uint64_t, Tuned> tuned;
     bool profiling = false;
@@ -131,6 +133,8 @@ inline int check_params(kwg_ctx* ctx, const kwg_fd1d_params* p)
         return set_err(ctx, KWG_ERR_INVALID, "kwg: block_warps must be 0, 1, 2 or 4");
     if (p->option_warps != 0 && p->option_warps != 1 && p->option_warps != 2 && p->option_warps != 4)
         return set_err(ctx, KWG_ERR_INVALID, "kwg: option_warps must be 0, 1, 2 or 4");
+    if (p->sm_blocks < 0 || p->sm_blocks > 64)
+        return set_err(ctx, KWG_ERR_INVALID, "kwg: sm_blocks must be in [0, 64]");
     return KWG_OK;
 }
 
@@ -160,8 +164,9 @@ inline double time_solve(kwg_ctx* ctx, F&& call)
 }
 
 // Times every candidate launch shape on fn(params) and returns the fastest: FP64 --
-// the streaming solver with 1, 2, 4 warps per block and the warp-per-PDE solver
-// (when pcr_ok); FP32 -- 1 and 2 warps per option.
+// the streaming solver with 1, 2, 4 warps per block (as many blocks per SM as fit),
+// with one 4-warp block per SM (one warp per scheduler), and the warp-per-PDE solver
+// (when pcr_ok); FP32 -- 1, 2 and 4 warps per option.
 template <typename F>
 inline kwg_ctx::Tuned tune(kwg_ctx* ctx, const kwg_fd1d_params* p, bool pcr_ok, F&& fn, kwg_tuning* out)
 {
@@ -169,16 +174,18 @@ inline kwg_ctx::Tuned tune(kwg_ctx* ctx, const kwg_fd1d_params* p, bool pcr_ok, 
     for (double& v : r.thomas_ms) v = -1.;
     r.pcr_ms = -1.;
     for (double& v : r.fp32_ms) v = -1.;
+    r.spread_ms = -1.;
     kwg_fd1d_params q = *p;
     q.strict = 0;
     kwg_ctx::Tuned best;
     double best_ms = -1.;
-    auto consider = [&](double ms, int solver, int bw, int ow) {
+    auto consider = [&](double ms, int solver, int bw, int ow, int sb) {
         if (ms >= 0. && (best_ms < 0. || ms < best_ms)) {
             best_ms = ms;
             best.solver = solver;
             best.block_warps = bw;
             best.option_warps = ow;
+            best.sm_blocks = sb;
         }
     };
     if (p->precision == KWG_FP64) {
@@ -186,26 +193,33 @@ inline kwg_ctx::Tuned tune(kwg_ctx* ctx, const kwg_fd1d_params* p, bool pcr_ok, 
         for (int i = 0; i < 3; ++i) {
             q.solver = KWG_SOLVER_THOMAS;
             q.block_warps = bws[i];
+            q.sm_blocks = 0;
             r.thomas_ms[i] = time_solve(ctx, [&] { return fn(q); });
-            consider(r.thomas_ms[i], KWG_SOLVER_THOMAS, bws[i], 1);
+            consider(r.thomas_ms[i], KWG_SOLVER_THOMAS, bws[i], 1, 0);
         }
+        q.block_warps = 4;
+        q.sm_blocks = 1;
+        r.spread_ms = time_solve(ctx, [&] { return fn(q); });
+        consider(r.spread_ms, KWG_SOLVER_THOMAS, 4, 1, 1);
         if (pcr_ok) {
             q.solver = KWG_SOLVER_PCR;
             q.block_warps = 0;
+            q.sm_blocks = 0;
             r.pcr_ms = time_solve(ctx, [&] { return fn(q); });
-            consider(r.pcr_ms, KWG_SOLVER_PCR, 1, 1);
+            consider(r.pcr_ms, KWG_SOLVER_PCR, 1, 1, 0);
         }
     } else {
         const int ws[3] = {1, 2, 4};
         for (int i = 0; i < 3; ++i) {
             q.option_warps = ws[i];
             r.fp32_ms[i] = time_solve(ctx, [&] { return fn(q); });
-            consider(r.fp32_ms[i], KWG_SOLVER_PCR, 1, ws[i]);
+            consider(r.fp32_ms[i], KWG_SOLVER_PCR, 1, ws[i], 0);
         }
     }
     r.solver = best.solver;
     r.block_warps = best.block_warps;
     r.option_warps = best.option_warps;
+    r.sm_blocks = best.sm_blocks;
     if (out) *out = r;
     return best;
 }

@@ -114,7 +114,10 @@ extern "C" int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const
                 (tn.solver != KWG_SOLVER_PCR || kwg::fd1d_pcr64_nodes_per_lane(x_max) > 0))
                 q.solver = tn.solver;
         }
-        if (q.block_warps) tn.block_warps = q.block_warps;
+        if (q.block_warps || q.sm_blocks) {
+            if (q.block_warps) tn.block_warps = q.block_warps;
+            tn.sm_blocks = q.sm_blocks;
+        }
         if (q.option_warps) tn.option_warps = q.option_warps;
     }
     const bool pcr = q.precision == KWG_FP32 || q.solver == KWG_SOLVER_PCR;
@@ -261,6 +264,7 @@ extern "C" int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const
     kwg::Fd1dShape sh = make_shape(&q);
     sh.block_warps = tn.block_warps;
     sh.option_warps = tn.option_warps;
+    sh.sm_blocks = tn.sm_blocks;
     sh.pde_x = (const int32_t*)(io + L.px);
     sh.pde_t = (const int32_t*)(io + L.pt);
     if (!pcr) {
@@ -277,7 +281,8 @@ extern "C" int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const
         int launches = 0;
         cudaMemcpyAsync(ctx->d_io, ctx->h_io, L.in_bytes, cudaMemcpyHostToDevice, st);
         if (!pcr) {
-            const int blocks = kwg::fd1d_fp64_solve_blocks((int)tiles.size(), ctx->device, sh.block_warps);
+            const int blocks = kwg::fd1d_fp64_solve_blocks((int)tiles.size(), ctx->device, sh.block_warps,
+                                                         sh.sm_blocks);
             launches += kwg::fd1d_fp64_launch(b, a, sh, (double*)ctx->d_work, d_pde_status, ctx->d_counter, d_prices,
                                               d_status, blocks, st, ctx->next_events());
         } else {
@@ -319,6 +324,7 @@ extern "C" int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const
 
     uint64_t sig = 0x5eed;
     for (uint64_t v : {(uint64_t)q.precision, (uint64_t)pcr, (uint64_t)sh.block_warps, (uint64_t)sh.option_warps,
+                       (uint64_t)sh.sm_blocks,
                        (uint64_t)n, (uint64_t)ms, (uint64_t)tiles.size(),
                        (uint64_t)node_lanes, (uint64_t)(uintptr_t)ctx->d_io, (uint64_t)(uintptr_t)ctx->d_work,
                        (uint64_t)(uintptr_t)ctx->h_io})

@@ -55,6 +55,7 @@ class Fd1dParams(ctypes.Structure):
         ("device_dedup", ctypes.c_int32),
         ("block_warps", ctypes.c_int32),
         ("option_warps", ctypes.c_int32),
+        ("sm_blocks", ctypes.c_int32),
     ]
 
 
@@ -80,16 +81,18 @@ class Tuning(ctypes.Structure):
         ("solver", ctypes.c_int32),
         ("block_warps", ctypes.c_int32),
         ("option_warps", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("sm_blocks", ctypes.c_int32),
         ("thomas_ms", ctypes.c_double * 3),
         ("pcr_ms", ctypes.c_double),
         ("fp32_ms", ctypes.c_double * 3),
+        ("spread_ms", ctypes.c_double),
     ]
 
     def as_dict(self) -> dict:
         return {"solver": {SOLVER_THOMAS: "thomas", SOLVER_PCR: "pcr"}.get(self.solver, self.solver),
-                "block_warps": self.block_warps, "option_warps": self.option_warps,
+                "block_warps": self.block_warps, "option_warps": self.option_warps, "sm_blocks": self.sm_blocks,
                 "thomas_ms_by_block_warps": {1: self.thomas_ms[0], 2: self.thomas_ms[1], 4: self.thomas_ms[2]},
+                "thomas_ms_one_4warp_block_per_sm": self.spread_ms,
                 "pcr_ms": self.pcr_ms,
                 "fp32_ms_by_option_warps": {1: self.fp32_ms[0], 2: self.fp32_ms[1], 4: self.fp32_ms[2]}}
 
@@ -544,11 +547,11 @@ class PricerFactory:
 
 
 def params(t_dim=512, x_dim=512, theta=0.5, scale=50.0, density=0.25, precision=FP64, solver=SOLVER_AUTO,
-           strict=0, block_warps=0, option_warps=0) -> Fd1dParams:
+           strict=0, block_warps=0, option_warps=0, sm_blocks=0) -> Fd1dParams:
     p = default_params()
     p.t_dim, p.x_dim, p.theta, p.scale, p.density = t_dim, x_dim, theta, scale, density
     p.precision, p.solver, p.strict = precision, solver, strict
-    p.block_warps, p.option_warps = block_warps, option_warps
+    p.block_warps, p.option_warps, p.sm_blocks = block_warps, option_warps, sm_blocks
     return p
 
 

@@ -35,6 +35,39 @@ def test_option_layout_matches_kw_option():
     assert kwg.OPTION_DTYPE.fields["e"][1] == 48 and kwg.OPTION_DTYPE.fields["w"][1] == 49
 
 
+def test_ctypes_mirrors_match_the_header(tmp_path):
+    """Size and every field offset of the structs in include/kwg.h, from a C program
+    compiled against the header, equal those of the ctypes mirrors in kwg.py."""
+    import kwg
+
+    structs = {"kwg_option": None, "kwg_fd1d_params": kwg.Fd1dParams, "kwg_tuning": kwg.Tuning,
+               "kwg_audit": kwg.Audit}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "kwg.h"', "int main(void) {"]
+    for name, cls in structs.items():
+        lines.append(f'printf("{name} size %zu\\n", sizeof({name}));')
+        fields = [f[0] for f in cls._fields_] if cls else list(kwg.OPTION_DTYPE.names)
+        for f in fields:
+            lines.append(f'printf("{name} {f} %zu\\n", offsetof({name}, {f}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        name, field, value = line.split()
+        got[(name, field)] = int(value)
+    for name, cls in structs.items():
+        if cls is None:
+            assert got[(name, "size")] == kwg.OPTION_DTYPE.itemsize
+            for f in kwg.OPTION_DTYPE.names:
+                assert got[(name, f)] == kwg.OPTION_DTYPE.fields[f][1], (name, f)
+            continue
+        assert got[(name, "size")] == ctypes.sizeof(cls), name
+        for f in cls._fields_:
+            assert got[(name, f[0])] == getattr(cls, f[0]).offset, (name, f[0])
+
+
 def test_params_default_is_reference_default(built):
     import kwg
 
