@@ -345,6 +345,73 @@ __device__ void drain(const Ring& r, uint32_t from, uint32_t to)
     for (uint32_t q = from; q < to; ++q) mbar_wait(&r.bar[q % kRing], (q / kRing) & 1u);
 }
 
+// Loads one full stage (kGroup nodes) into registers, refills its ring slot, and runs
+// the stage's node-steps: the elimination recurrence yh, the new value with the
+// early-exercise floor, the second recurrence f, and the 16-byte (value, f) store of
+// each node.  kCompact: the stage lies in the frozen middle region (coefficients
+// ca, cb, cs).  No per-node guard: the unrolled stage is one block the scheduler
+// interleaves across nodes.
+template <bool kUp, bool kHalf, bool kCompact>
+__device__ __forceinline__ void stage_body(const Ring& ring, uint32_t v, const TileView& tv, int g, int ng, int N,
+                                           const Ranges& rg, int first, bool pfree, const unsigned char* st, int lane,
+                                           double ca, double cb, double cs, double c, bool amer, bool active,
+                                           double2* sout, double& yh, double& f)
+{
+    const double* sc_ = reinterpret_cast<const double*>(st) + lane;
+    const double* sp_ = reinterpret_cast<const double*>(st + kStageCoef) + lane;
+    const double2* ss_ = reinterpret_cast<const double2*>(st + kStageCoef + kStageP) + lane;
+    double ra[kGroup], rb[kGroup], rs[kGroup], rp[kGroup], rv[kGroup], rw[kGroup];
+#pragma unroll
+    for (int k = 0; k < kGroup; ++k) {
+        const int idx = kUp ? k : kGroup - 1 - k;  // processing order within the stage
+        rp[k] = pfree ? 0. : sp_[idx * kTile];
+        const double2 sv = ss_[idx * kTile];
+        rv[k] = sv.x;
+        rw[k] = sv.y;
+        ra[k] = kCompact ? ca : sc_[(idx * kCoef + 0) * kTile];
+        rb[k] = kCompact ? cb : sc_[(idx * kCoef + 1) * kTile];
+        rs[k] = kCompact ? cs : sc_[(idx * kCoef + 2) * kTile];
+    }
+    __syncwarp();  // the slot fully read before it is refilled
+    if (lane == 0 && g + kRing < ng) issue<kUp>(ring, v + kRing, tv, g + kRing, N, rg);
+#pragma unroll
+    for (int k = 0; k < kGroup; ++k) {
+        const int j = kUp ? first + k : first + kGroup - 1 - k;
+        yh = fma(-ra[k], yh, rw[k]);
+        double vn = kHalf ? fma(rs[k], yh, -rv[k]) : fma(rs[k], yh, -c * rv[k]);
+        if (amer && j < N - 1) vn = max_floor(vn, rp[k]);
+        f = fma(-rb[k], f, vn);
+        if (active) sout[(size_t)j * kTile] = make_double2(vn, f);
+    }
+}
+
+// A sweep's last stage when it holds fewer than kGroup nodes.  It refills no ring
+// slot (no later stage), so it reads shared memory node by node in a rolled loop
+// and holds no stage in registers.
+template <bool kUp, bool kHalf>
+__device__ __forceinline__ void tail_stage(int first, int count, bool compact, bool pfree, const unsigned char* st,
+                                           int lane, double ca, double cb, double cs, double c, bool amer,
+                                           bool active, int N, double2* sout, double& yh, double& f)
+{
+    const double* sc_ = reinterpret_cast<const double*>(st) + lane;
+    const double* sp_ = reinterpret_cast<const double*>(st + kStageCoef) + lane;
+    const double2* ss_ = reinterpret_cast<const double2*>(st + kStageCoef + kStageP) + lane;
+#pragma unroll 1
+    for (int k = 0; k < count; ++k) {
+        const int idx = kUp ? k : count - 1 - k;
+        const int j = first + idx;
+        const double2 sv = ss_[idx * kTile];
+        const double a = compact ? ca : sc_[(idx * kCoef + 0) * kTile];
+        const double bb = compact ? cb : sc_[(idx * kCoef + 1) * kTile];
+        const double sg = compact ? cs : sc_[(idx * kCoef + 2) * kTile];
+        yh = fma(-a, yh, sv.y);
+        double vn = kHalf ? fma(sg, yh, -sv.x) : fma(sg, yh, -c * sv.x);
+        if (amer && j < N - 1) vn = max_floor(vn, pfree ? 0. : sp_[idx * kTile]);
+        f = fma(-bb, f, vn);
+        if (active) sout[(size_t)j * kTile] = make_double2(vn, f);
+    }
+}
+
 // One sweep over this warp's tile.  Returns false on a wait timeout (already drained).
 template <bool kUp, bool kHalf>
 __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileView& tv, int lane, int N,
@@ -379,36 +446,15 @@ __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileVi
         const bool compact = stage_compact(first, count, rg.lo, rg.hi);
         const bool pfree = stage_compact(first, count, rg.zlo, rg.zhi);
         const unsigned char* st = ring.stage + (size_t)s * kStageBytes;
-        const double* sc_ = reinterpret_cast<const double*>(st) + lane;
-        const double* sp_ = reinterpret_cast<const double*>(st + kStageCoef) + lane;
-        const double2* ss_ = reinterpret_cast<const double2*>(st + kStageCoef + kStageP) + lane;
-        double ra[kGroup], rb[kGroup], rs[kGroup], rp[kGroup], rv[kGroup], rw[kGroup];
-#pragma unroll
-        for (int k = 0; k < kGroup; ++k) {
-            const int idx = kUp ? k : count - 1 - k;  // processing order within the stage
-            if (k < count) {
-                rp[k] = pfree ? 0. : sp_[idx * kTile];
-                const double2 sv = ss_[idx * kTile];
-                rv[k] = sv.x;
-                rw[k] = sv.y;
-                ra[k] = compact ? ca : sc_[(idx * kCoef + 0) * kTile];
-                rb[k] = compact ? cb : sc_[(idx * kCoef + 1) * kTile];
-                rs[k] = compact ? cs : sc_[(idx * kCoef + 2) * kTile];
-            }
-        }
-        __syncwarp();  // stage s fully read before it is refilled
-        if (lane == 0 && g + kRing < ng) issue<kUp>(ring, v + kRing, tv, g + kRing, N, rg);
-#pragma unroll
-        for (int k = 0; k < kGroup; ++k) {
-            if (k < count) {
-                const int j = kUp ? first + k : first + count - 1 - k;
-                yh = fma(-ra[k], yh, rw[k]);
-                double vn = kHalf ? fma(rs[k], yh, -rv[k]) : fma(rs[k], yh, -c * rv[k]);
-                if (amer && j < N - 1) vn = max_floor(vn, rp[k]);
-                f = fma(-rb[k], f, vn);
-                if (active) sout[(size_t)j * kTile] = make_double2(vn, f);
-            }
-        }
+        if (count == kGroup && compact)
+            stage_body<kUp, kHalf, true>(ring, v, tv, g, ng, N, rg, first, pfree, st, lane, ca, cb, cs, c, amer,
+                                         active, sout, yh, f);
+        else if (count == kGroup)
+            stage_body<kUp, kHalf, false>(ring, v, tv, g, ng, N, rg, first, pfree, st, lane, ca, cb, cs, c, amer,
+                                          active, sout, yh, f);
+        else
+            tail_stage<kUp, kHalf>(first, count, compact, pfree, st, lane, ca, cb, cs, c, amer, active, N, sout, yh,
+                                   f);
     }
     return true;
 }
