@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include "fd1d_kernels.h"
+#include "host_dedup.h"
 #include "kwg.h"
 #include "kwg_ctx.h"
 #include "tma.cuh"
@@ -343,26 +344,10 @@ int price_host(kwg_ctx* ctx, const kwg_option* user_opts, size_t n_user, const k
         n = 2 * n_user;
     }
 
-    // 1. dedup (src/Pricer/kwFd1d.cpp:28-65): sort by (t, r, q, z, e, w).
-    auto key = [&](uint32_t i) {
-        const kwg_option& o = opts[i];
-        return std::tie(o.t, o.r, o.q, o.z, o.e, o.w);
-    };
-    std::vector<uint32_t> order(n);
-    std::iota(order.begin(), order.end(), 0u);
-    std::sort(order.begin(), order.end(), [&](uint32_t l, uint32_t r) { return key(l) < key(r); });
-    std::vector<int32_t> asset2pde(n);
+    // 1. dedup by the reference's key (t, r, q, z, e, w), src/Pricer/kwFd1d.cpp:28-65
+    std::vector<int32_t> asset2pde;
     std::vector<uint32_t> pde2asset;
-    pde2asset.reserve(n);
-    pde2asset.push_back(order[0]);
-    asset2pde[order[0]] = 0;
-    for (size_t i = 1; i < n; ++i) {
-        const uint32_t l = order[i - 1], r = order[i];
-        const bool equal = (key(l) < key(r)) == (key(r) < key(l));
-        if (!equal) pde2asset.push_back(r);
-        asset2pde[r] = (int32_t)(pde2asset.size() - 1);
-    }
-    const size_t m = pde2asset.size();
+    const size_t m = kwg::dedup_host(opts, n, nullptr, nullptr, asset2pde, pde2asset);
     const size_t m_pad = (m + kwg::kTile - 1) / kwg::kTile * kwg::kTile;
     // PDEs grouped by exercise / put-call class (stable), so tiles are homogeneous
     {

@@ -15,6 +15,7 @@
 //   * the device sequence (H2D copy, kernels, D2H copy) is captured once into a CUDA
 //     graph and replayed while the batch layout stays the same.
 #include <algorithm>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <numeric>
@@ -24,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include "fd1d_kernels.h"
+#include "host_dedup.h"
 #include "kwg.h"
 #include "kwg_ctx.h"
 
@@ -124,24 +126,9 @@ extern "C" int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const
     KWG_CUDA(ctx, cudaSetDevice(ctx->device));
 
     // 1. dedup by (t, r, q, z, e, w, x_dim, t_dim)
-    auto key = [&](uint32_t i) {
-        const kwg_option& o = opts[i];
-        return std::tie(o.t, o.r, o.q, o.z, o.e, o.w, x_dims[i], t_dims[i]);
-    };
-    std::vector<uint32_t> order(n);
-    std::iota(order.begin(), order.end(), 0u);
-    std::sort(order.begin(), order.end(), [&](uint32_t l, uint32_t r) { return key(l) < key(r); });
-    std::vector<int32_t> asset2pde(n);
+    std::vector<int32_t> asset2pde;
     std::vector<uint32_t> pde2asset;
-    pde2asset.reserve(n);
-    pde2asset.push_back(order[0]);
-    asset2pde[order[0]] = 0;
-    for (size_t i = 1; i < n; ++i) {
-        const uint32_t l = order[i - 1], r = order[i];
-        if (key(l) < key(r) || key(r) < key(l)) pde2asset.push_back(r);
-        asset2pde[r] = (int32_t)(pde2asset.size() - 1);
-    }
-    const size_t m = pde2asset.size();
+    const size_t m = kwg::dedup_host(opts, n, x_dims, t_dims, asset2pde, pde2asset);
     auto xd = [&](size_t pde) { return x_dims[pde2asset[pde]]; };
     auto td = [&](size_t pde) { return t_dims[pde2asset[pde]]; };
 
@@ -154,12 +141,18 @@ extern "C" int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const
     std::vector<int> bucket_x;
     std::vector<bool> bucket_full;
     long long node_lanes = 0;
+    // PDEs in layout order: sorted on one packed integer key per PDE (ties by PDE
+    // number, so the layout is deterministic)
     std::vector<uint32_t> by(m);
-    std::iota(by.begin(), by.end(), 0u);
+    auto sort_by = [&](auto packed_key) {
+        std::vector<std::pair<uint64_t, uint32_t>> kv(m);
+        for (size_t i = 0; i < m; ++i) kv[i] = {packed_key((uint32_t)i), (uint32_t)i};
+        kwg::radix_sort_pairs(kv);
+        for (size_t i = 0; i < m; ++i) by[i] = kv[i].second;
+    };
     if (!pcr) {
-        std::sort(by.begin(), by.end(), [&](uint32_t a, uint32_t b) {
-            return std::make_tuple(xd(a), -td(a)) < std::make_tuple(xd(b), -td(b));
-        });
+        // x_dim ascending, t_dim descending
+        sort_by([&](uint32_t p) { return (uint64_t)(uint32_t)xd(p) << 32 | (uint32_t)(INT32_MAX - td(p)); });
         struct Chunk {
             size_t begin, count;
             int x, tmax;
@@ -191,9 +184,11 @@ extern "C" int kwg_fd1d_price_uneven(kwg_ctx* ctx, const kwg_option* opts, const
             return q.precision == KWG_FP32 ? kwg::fd1d_fp32_nodes_per_lane(xd(pde))
                                            : kwg::fd1d_pcr64_nodes_per_lane(xd(pde));
         };
-        std::sort(by.begin(), by.end(), [&](uint32_t a, uint32_t b) {
-            return std::make_tuple(mlane(a), -(long long)xd(a) * (td(a) - 1)) <
-                   std::make_tuple(mlane(b), -(long long)xd(b) * (td(b) - 1));
+        // nodes per lane ascending, node-steps descending (x_dim <= 2048 here, so
+        // node-steps < 2^43)
+        sort_by([&](uint32_t p) {
+            const uint64_t work = (uint64_t)xd(p) * (uint64_t)(td(p) > 1 ? td(p) - 1 : 0);
+            return (uint64_t)(mlane(p) + 1) << 50 | (((1ull << 50) - 1) - work);
         });
         long long off = 0;
         for (size_t i = 0; i < m; ++i) {

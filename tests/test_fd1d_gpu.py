@@ -151,6 +151,35 @@ def test_bad_option_fields(ctx, solver):
     assert (st[[0, 2, 3, 4, 6]] == 0).all()
 
 
+@pytest.mark.parametrize("api", ["host", "uneven"])
+def test_nan_key_never_merges(ctx, api):
+    """Dedup compares keys by value: an option whose vol is NaN matches nothing, so it
+    keeps its own PDE and reports bad input, while its otherwise identical twin (and
+    a -0.0 / +0.0 rate pair, equal by value) price normally."""
+    import kwg
+    import portfolio
+
+    o = portfolio.american_portfolio(8, seed=21)
+    o[1] = o[0]
+    o[1]["z"] = np.nan
+    o[2] = o[0]
+    o[3] = o[0]
+    o[2]["r"] = 0.0
+    o[3]["r"] = -0.0
+    prm = kwg.params(t_dim=64, x_dim=128, scale=5.0)
+    if api == "host":
+        rc, p, st = ctx.fd1d_price(o, prm)
+    else:
+        xd = np.full(len(o), 128, np.int32)
+        td = np.full(len(o), 64, np.int32)
+        rc, p, st = ctx.fd1d_price_uneven(o, xd, td, prm)
+    assert rc == kwg.KWG_OK
+    assert st[1] == kwg.STATUS_BAD_INPUT and np.isnan(p[1])
+    keep = np.arange(len(o)) != 1
+    assert (st[keep] == 0).all() and np.isfinite(p[keep]).all()
+    assert p[2] == p[3]
+
+
 def test_device_api_matches_host_api(ctx):
     import torch
 
