@@ -191,7 +191,7 @@ int kwg_autotune_uneven(kwg_ctx* ctx, const kwg_option* opts, const int32_t* x_d
                         size_t n, const kwg_fd1d_params* p, kwg_tuning* out);
 
 /* Compact form of kwg_autotune_ex for FP64: tunes and records the same choices and
- * writes the best streaming (Thomas) solve time over the block sizes and the
+ * writes the best streaming (Thomas) solve time over the block sizes and residencies and the
  * warp-per-PDE (PCR) solve time (ms; negative if not applicable).  The choice is kept
  * for calls of the same shape (precision, x_dim, t_dim, m rounded to a power of two)
  * on this context.  No counterpart in the reference, which has one CPU solver. */

@@ -627,6 +627,7 @@ int kwg_autotune(kwg_ctx* ctx, const kwg_fd1d_params* p, size_t m, double* thoma
     double best = -1.;
     for (double v : t.thomas_ms)
         if (v >= 0. && (best < 0. || v < best)) best = v;
+    if (t.spread_ms >= 0. && (best < 0. || t.spread_ms < best)) best = t.spread_ms;
     if (thomas_ms) *thomas_ms = best;
     if (pcr_ms) *pcr_ms = t.pcr_ms;
     return KWG_OK;
