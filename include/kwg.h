@@ -97,6 +97,17 @@ typedef struct kwg_ctx kwg_ctx;
 /* Fills p with the reference defaults (src/Pricer/kwFd1d.cpp:12-16, kwFd1d.h:31). */
 void kwg_fd1d_params_default(kwg_fd1d_params* p);
 
+/* The grouping of options into PDEs that every pricing call uses
+ * (src/Pricer/kwFd1d.cpp:28-65): options with equal (t, r, q, z, e, w) -- and, when
+ * x_dims and t_dims are given (uneven batches), equal grid shape -- share one PDE.
+ * Writes asset2pde[n] (each option's PDE; PDEs are numbered in order of their first
+ * option) and, unless pde2asset is NULL, pde2asset[m] (each PDE's first option; room
+ * for n entries); returns m.  Keys compare by value (+0 == -0); a NaN field matches
+ * nothing, so such an option keeps its own PDE.  Host only: no context, no GPU.
+ * O(n) (the reference sorts, O(n log n)). */
+size_t kwg_fd1d_dedup(const kwg_option* opts, const int32_t* x_dims, const int32_t* t_dims, size_t n,
+                      int32_t* asset2pde, uint32_t* pde2asset);
+
 /* Creates a context on CUDA device `device`; NULL on failure (no GPU, bad id). */
 kwg_ctx* kwg_create(int device);
 void kwg_destroy(kwg_ctx* ctx);

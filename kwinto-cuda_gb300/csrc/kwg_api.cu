@@ -598,6 +598,19 @@ int kwg_selftest_waits(kwg_ctx* ctx, int32_t* timed_out, int32_t* completed)
     return KWG_OK;
 }
 
+size_t kwg_fd1d_dedup(const kwg_option* opts, const int32_t* x_dims, const int32_t* t_dims, size_t n,
+                      int32_t* asset2pde, uint32_t* pde2asset)
+{
+    if (!opts || !asset2pde || n == 0) return 0;
+    std::vector<int32_t> a2p;
+    std::vector<uint32_t> p2a;
+    const size_t m = kwg::dedup_host(opts, n, x_dims && t_dims ? x_dims : nullptr, x_dims && t_dims ? t_dims : nullptr,
+                                     a2p, p2a);
+    std::memcpy(asset2pde, a2p.data(), n * sizeof(int32_t));
+    if (pde2asset) std::memcpy(pde2asset, p2a.data(), m * sizeof(uint32_t));
+    return m;
+}
+
 int kwg_autotune_ex(kwg_ctx* ctx, const kwg_fd1d_params* p, size_t m, kwg_tuning* out)
 {
     if (!ctx) return KWG_ERR_INVALID;

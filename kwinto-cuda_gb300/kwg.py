@@ -111,6 +111,8 @@ def lib() -> ctypes.CDLL:
     vp, sz, i32, dp = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p
     L.kwg_fd1d_params_default.argtypes = [ctypes.POINTER(Fd1dParams)]
     L.kwg_fd1d_params_default.restype = None
+    L.kwg_fd1d_dedup.argtypes = [vp, vp, vp, sz, vp, vp]
+    L.kwg_fd1d_dedup.restype = sz
     L.kwg_create.argtypes = [i32]
     L.kwg_create.restype = vp
     L.kwg_destroy.argtypes = [vp]
@@ -164,6 +166,27 @@ def lib() -> ctypes.CDLL:
     L.kwg_surrogate_price.restype = i32
     _lib = L
     return L
+
+
+def dedup(opts, x_dims=None, t_dims=None) -> tuple[np.ndarray, np.ndarray]:
+    """The PDE grouping every pricing call uses (kwg_fd1d_dedup; the reference's key,
+    src/Pricer/kwFd1d.cpp:28-65, plus the grid shape when x_dims/t_dims are given):
+    (asset2pde, pde2asset).  Host only."""
+    o = np.ascontiguousarray(opts, dtype=OPTION_DTYPE)
+    n = len(o)
+    a2p = np.zeros(n, np.int32)
+    p2a = np.zeros(n, np.uint32)
+    if n == 0:
+        return a2p, p2a
+    xp = tp = None
+    if x_dims is not None and t_dims is not None:
+        xd = np.ascontiguousarray(x_dims, np.int32)
+        td = np.ascontiguousarray(t_dims, np.int32)
+        if xd.shape != (n,) or td.shape != (n,):
+            raise ValueError("dedup: x_dims and t_dims need one entry per option")
+        xp, tp = xd.ctypes.data, td.ctypes.data
+    m = lib().kwg_fd1d_dedup(o.ctypes.data, xp, tp, n, a2p.ctypes.data, p2a.ctypes.data)
+    return a2p, p2a[:m].copy()
 
 
 def default_params() -> Fd1dParams:

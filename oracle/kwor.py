@@ -65,6 +65,8 @@ def oracle_lib():
         L.kwor_bs_price.restype = None
         L.kwor_fd1d_solve_grid.argtypes = [vp, ctypes.POINTER(OracleParams), vp, vp]
         L.kwor_fd1d_solve_grid.restype = ctypes.c_int
+        L.kwor_dedup.argtypes = [vp, sz, vp, vp]
+        L.kwor_dedup.restype = sz
         _oracle = L
     return _oracle
 
@@ -110,6 +112,16 @@ def fd1d_price(opts: np.ndarray, nthreads: int = 0, bs: bool = False, **kw):
     rc = fn(opts.ctypes.data, n, ctypes.byref(p), nthreads or os.cpu_count() or 1, prices.ctypes.data,
             status.ctypes.data, err, 512)
     return rc, err.value.decode(), prices, status
+
+
+def dedup(opts: np.ndarray):
+    """kwor_dedup (src/Pricer/kwFd1d.cpp:28-65): (asset2pde, pde2asset), PDEs in key order."""
+    o = _as_options(opts)
+    n = len(o)
+    a2p = np.zeros(n, np.uint32)
+    p2a = np.zeros(n, np.uint32)
+    m = oracle_lib().kwor_dedup(o.ctypes.data, n, a2p.ctypes.data, p2a.ctypes.data) if n else 0
+    return a2p, p2a[:m].copy()
 
 
 def bs_price(opts: np.ndarray) -> np.ndarray:

@@ -68,6 +68,63 @@ def test_ctypes_mirrors_match_the_header(tmp_path):
             assert got[(name, f[0])] == getattr(cls, f[0]).offset, (name, f[0])
 
 
+def _canonical(a2p):
+    """Group labels renumbered by first occurrence, so equal partitions compare equal."""
+    first = {}
+    return np.array([first.setdefault(int(g), len(first)) for g in a2p])
+
+
+def test_dedup_matches_the_oracle(built):
+    """The hash-table dedup every pricing call uses groups options exactly as the
+    oracle's restatement of the reference's sort (src/Pricer/kwFd1d.cpp:28-65):
+    repeated keys, keys that differ only in spot or strike, and +0.0 / -0.0 rates."""
+    import sys
+
+    import kwg
+    import portfolio
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import kwor
+
+    rng = np.random.default_rng(1)
+    o = portfolio.american_portfolio(3000, seed=8)
+    dup = o[rng.integers(0, len(o), 2000)]
+    dup["s"][:500] *= 1.1
+    dup["k"][500:1000] *= 0.9
+    zp = o[:10].copy()
+    zp["r"] = 0.0
+    zm = zp.copy()
+    zm["r"] = -0.0
+    o = np.concatenate([o, dup, zp, zm])
+    o = o[rng.permutation(len(o))]
+    a2p, p2a = kwg.dedup(o)
+    ra2p, rp2a = kwor.dedup(o)
+    assert len(p2a) == len(rp2a) < len(o)
+    assert np.array_equal(_canonical(a2p), _canonical(ra2p))
+    assert (a2p[p2a] == np.arange(len(p2a))).all()  # each PDE's first option maps to it
+    assert (np.diff(p2a.astype(np.int64)) > 0).all()  # PDEs numbered by first option
+
+
+def test_dedup_nan_keys_and_grid_shapes(built):
+    """A NaN field matches nothing (the reference's sort would merge such a key with
+    a neighbour); with per-option grid shapes, equal keys on different grids are
+    different PDEs."""
+    import kwg
+    import portfolio
+
+    o = portfolio.american_portfolio(4, seed=3)
+    o = np.concatenate([o, o])
+    o["z"][[1, 5]] = np.nan
+    a2p, p2a = kwg.dedup(o)
+    assert a2p[0] == a2p[4] and a2p[2] == a2p[6] and a2p[3] == a2p[7]
+    assert a2p[1] != a2p[5] and len(p2a) == 5
+    xd = np.array([128] * 4 + [256] * 4, np.int32)
+    td = np.full(8, 64, np.int32)
+    a2p2, p2a2 = kwg.dedup(o, xd, td)
+    assert len(p2a2) == 8 and len(set(a2p2.tolist())) == 8
+    assert kwg.dedup(o[:0])[1].size == 0
+
+
 def test_params_default_is_reference_default(built):
     import kwg
 
