@@ -1,5 +1,5 @@
-// fd1d_fp32.cu -- FP32 stepping with FP64-accurate state: one or two warps per PDE
-// (tuned; always two for grids of 1025..2048 nodes), the whole PDE on chip (state in
+// fd1d_fp32.cu -- FP32 stepping with FP64-accurate state: one, two or four warps per
+// PDE (tuned; at least two for grids of 1025..2048 nodes), the whole PDE on chip (state in
 // registers, coefficient tables in shared memory), a partitioned tridiagonal solve
 // with a cyclic reduction of the separator system (warp shuffles; shared memory
 // across the warps of a PDE).
