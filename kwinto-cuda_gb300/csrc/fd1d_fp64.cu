@@ -42,7 +42,10 @@
 // and where the payoff of every lane of the tile is exactly +0 (the out-of-the-money
 // side of a tile of puts only or calls only; all nodes of European PDEs, which never
 // project) the payoff is not read either: the projection there is max(V, +0).
+#include <atomic>
 #include <cstdint>
+#include <mutex>
+
 #include <cuda_runtime.h>
 
 #include "fd1d_common.cuh"
@@ -592,38 +595,54 @@ __global__ void fd1d_interp_fp64(const PdeBatch b, const AssetBatch a, Fd1dShape
     if (status) status[i] = st;
 }
 
-int fd1d_fp64_solve_blocks(int ntiles, int device, int block_warps, int sm_blocks)
-{
-    // occupancy per block size (1, 2, 4 warps), cached for one device
-    static int cached_dev = -1, cached_sms = 0, cached_max[kMaxBlockWarps + 1] = {};
-    if (cached_dev != device) {
-        cudaDeviceGetAttribute(&cached_sms, cudaDevAttrMultiProcessorCount, device);
-        for (int bw = 1; bw <= kMaxBlockWarps; bw *= 2) {
-            cudaFuncSetAttribute(fd1d_solve_fp64<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(kMaxBlockWarps * kSolveSmem));
-            cudaFuncSetAttribute(fd1d_solve_fp64<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(kMaxBlockWarps * kSolveSmem));
-            int mx = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mx, fd1d_solve_fp64<true>, 32 * bw, bw * kSolveSmem);
-            cached_max[bw] = mx < 1 ? 1 : mx;
-        }
-        cached_dev = device;
-    }
-    const int bw = block_warps == 2 || block_warps == 4 ? block_warps : 1;
-    const int want = (ntiles + bw - 1) / bw;  // one tile per warp at most
-    const int per_sm = sm_blocks > 0 && sm_blocks < cached_max[bw] ? sm_blocks : cached_max[bw];
-    const int cap = cached_sms * per_sm;
-    return want < cap ? (want > 0 ? want : 1) : cap;
-}
+namespace {
+// Per-device launch facts, filled once under a lock by fd1d_prepare_kernels and read
+// without one afterwards (the ready flag publishes them).
+constexpr int kMaxDevices = 64;
+struct DeviceFacts {
+    int sms = 0;
+    int max_blocks[kMaxBlockWarps + 1] = {};  // FP64 streaming solver: blocks per SM by block size
+};
+DeviceFacts g_facts[kMaxDevices];
+std::atomic<bool> g_ready[kMaxDevices];
+std::mutex g_prepare_mu;
+}  // namespace
 
 void fd1d_prepare_kernels(int device)
 {
-    static bool done[64] = {};
-    if (device < 0 || device >= 64 || done[device]) return;
-    fd1d_fp64_solve_blocks(1, device);  // caches the FP64 kernel's occupancy
+    if (device < 0 || device >= kMaxDevices || g_ready[device].load(std::memory_order_acquire)) return;
+    std::lock_guard<std::mutex> lock(g_prepare_mu);
+    if (g_ready[device].load(std::memory_order_relaxed)) return;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    if (prev != device) cudaSetDevice(device);
+    DeviceFacts& f = g_facts[device];
+    cudaDeviceGetAttribute(&f.sms, cudaDevAttrMultiProcessorCount, device);
+    cudaFuncSetAttribute(fd1d_solve_fp64<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(kMaxBlockWarps * kSolveSmem));
+    cudaFuncSetAttribute(fd1d_solve_fp64<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(kMaxBlockWarps * kSolveSmem));
+    for (int bw = 1; bw <= kMaxBlockWarps; bw *= 2) {
+        int mx = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mx, fd1d_solve_fp64<true>, 32 * bw, bw * kSolveSmem);
+        f.max_blocks[bw] = mx < 1 ? 1 : mx;
+    }
     fd1d_fp32_prepare(device);
     fd1d_pcr64_prepare(device);
-    done[device] = true;
+    if (prev >= 0 && prev != device) cudaSetDevice(prev);
+    g_ready[device].store(true, std::memory_order_release);
+}
+
+int fd1d_fp64_solve_blocks(int ntiles, int device, int block_warps, int sm_blocks)
+{
+    if (device < 0 || device >= kMaxDevices) return 1;
+    fd1d_prepare_kernels(device);
+    const DeviceFacts& f = g_facts[device];
+    const int bw = block_warps == 2 || block_warps == 4 ? block_warps : 1;
+    const int want = (ntiles + bw - 1) / bw;  // one tile per warp at most
+    const int per_sm = sm_blocks > 0 && sm_blocks < f.max_blocks[bw] ? sm_blocks : f.max_blocks[bw];
+    const int cap = (f.sms > 0 ? f.sms : 1) * per_sm;
+    return want < cap ? (want > 0 ? want : 1) : cap;
 }
 
 size_t fd1d_fp64_work_bytes_nl(int m_pad, long long node_lanes)

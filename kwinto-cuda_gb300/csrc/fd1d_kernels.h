@@ -113,7 +113,10 @@ __global__ void fd1d_interp_rows(const PdeBatch b, const AssetBatch a, Fd1dShape
                                  int32_t* __restrict__ status);
 
 // One-time per-device set-up of every kernel's shared-memory limit and occupancy, so
-// that launches (also inside a stream capture) make no attribute calls.
+// that launches (also inside a stream capture) make no attribute calls.  Safe to call
+// from several threads: the first call for a device does the work under a lock, later
+// ones return after one atomic load.  fd1d_fp32_prepare and fd1d_pcr64_prepare run
+// only inside it.
 void fd1d_prepare_kernels(int device);
 void fd1d_fp32_prepare(int device);
 void fd1d_pcr64_prepare(int device);

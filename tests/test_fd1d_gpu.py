@@ -180,6 +180,60 @@ def test_nan_key_never_merges(ctx, api):
     assert p[2] == p[3]
 
 
+def test_contexts_on_threads_price_concurrently(built):
+    """One context per thread (the reference's pricers are not re-entrant either):
+    four threads price different portfolios at once, with both solvers, FP32 and an
+    uneven batch among them; every result equals the same call made alone."""
+    import threading
+
+    import kwg
+    import portfolio
+
+    jobs = [
+        ("price", portfolio.american_portfolio(3000, seed=31), kwg.params(t_dim=96, x_dim=256, scale=5.0, solver=1)),
+        ("price", portfolio.american_portfolio(500, seed=32), kwg.params(t_dim=64, x_dim=512, scale=5.0, solver=2)),
+        ("price", portfolio.american_portfolio(2000, seed=33),
+         kwg.params(t_dim=80, x_dim=1024, scale=5.0, precision=kwg.FP32)),
+        ("uneven",) + portfolio.uneven_portfolio(1500, seed=34) + (kwg.params(scale=5.0, density=math.inf),),
+    ]
+
+    def run(c, job):
+        if job[0] == "price":
+            rc, p, st = c.fd1d_price(job[1], job[2])
+        else:
+            _, o, xd, td, prm = job
+            rc, p, st = c.fd1d_price_uneven(o, np.minimum(xd, 512), np.minimum(td, 160), prm)
+        assert rc == kwg.KWG_OK, c.last_error()
+        return p, st
+
+    ctxs = [kwg.Context(0) for _ in jobs]
+    try:
+        alone = [run(c, j) for c, j in zip(ctxs, jobs)]
+        out = [None] * len(jobs)
+        errors = []
+
+        def worker(i):
+            try:
+                for _ in range(3):
+                    out[i] = run(ctxs[i], jobs[i])
+            except BaseException as e:  # noqa: BLE001 - reported below
+                errors.append(e)
+
+        threads = [threading.Thread(target=worker, args=(i,)) for i in range(len(jobs))]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        assert not errors, errors
+        for (pa, sa), (pb, sb) in zip(alone, out):
+            assert np.array_equal(sa, sb)
+            ok = sa == 0
+            assert np.array_equal(pa[ok], pb[ok])
+    finally:
+        for c in ctxs:
+            c.close()
+
+
 def test_device_api_matches_host_api(ctx):
     import torch
 
