@@ -284,6 +284,49 @@ def test_device_dedup_matches_host_dedup(ctx, precision, solver):
     assert np.isnan(got[~ok]).all()
 
 
+def test_million_option_batch(ctx):
+    """Maximum-size batch through both entry points: 2^20 options (a quarter of
+    them repeated keys), 64 x 64 grid.  Every option prices, the host call and the
+    device call with on-device dedup agree bit for bit, and a sample matches the
+    oracle."""
+    import sys
+
+    import torch
+
+    import kwg
+    import portfolio
+    from conftest import ROOT
+
+    sys.path.insert(0, f"{ROOT}/oracle")
+    import kwor
+
+    n = 1 << 20
+    o = portfolio.american_portfolio(3 * n // 4, seed=45)
+    rng = np.random.default_rng(5)
+    o = np.concatenate([o, o[rng.integers(0, len(o), n - len(o))]])
+    o = np.ascontiguousarray(o[rng.permutation(n)], dtype=kwg.OPTION_DTYPE)
+    kw = dict(t_dim=64, x_dim=64, scale=5.0, density=0.25)
+    rc, p, st = ctx.fd1d_price(o, kwg.params(**kw))
+    assert rc == 0, ctx.last_error()
+    assert (st == 0).all() and np.isfinite(p).all()
+    prm = kwg.params(**kw)
+    prm.device_dedup = 1
+    d_o = torch.from_numpy(o.view(np.uint8).copy()).cuda()
+    d_p = torch.empty(n, dtype=torch.float64, device="cuda")
+    d_s = torch.empty(n, dtype=torch.int32, device="cuda")
+    rc = ctx.fd1d_price_device(d_o.data_ptr(), n, prm, d_p.data_ptr(), d_s.data_ptr(),
+                               torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, ctx.last_error()
+    torch.cuda.synchronize()
+    assert np.array_equal(d_s.cpu().numpy(), st)
+    assert np.array_equal(d_p.cpu().numpy(), p)
+    idx = rng.choice(n, 48, replace=False)
+    rc, msg, want, _ = kwor.fd1d_price(o[idx], **kw)
+    assert rc == 0, msg
+    assert rel_err(p[idx], want) <= REL_TOL
+    del d_o, d_p, d_s
+
+
 def test_pricer_mirror(built):
     """kw::PricerFactory / kw::Pricer usage exactly like test/kwPricer_test.cpp:63-84."""
     import kwg
