@@ -37,11 +37,17 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 // table fields per node, layout [node-in-lane][field][lane] (conflict-free).  On a
-// uniform grid without padded nodes the residual coefficients c1..c4 are the same
-// at every interior node, so they live in registers and the table keeps 7 fields.
+// uniform grid without padded nodes the interior rows of B are the same at every
+// node, so
+//   * the residual coefficients c1..c4 live in registers;
+//   * every lane but the last has the same interior block B_I, hence the same LU
+//     factors and spikes: those 5 fields are kept once for the group plus once for
+//     the last lane (whose block holds the boundary row), [node][field][2], read as
+//     broadcasts; only the payoff pair stays per lane.
 enum { T_L = 0, T_ID, T_U, T_SL, T_SR, T_PH, T_PL, T_C1, T_C2, T_C3, T_C4 };
 template <bool kUni>
-__host__ __device__ constexpr int f32_fields() { return kUni ? 7 : 11; }
+__host__ __device__ constexpr int f32_fields() { return kUni ? 2 : 11; }  // per-lane fields
+constexpr int kSharedFields = 5;                                          // T_L .. T_SR
 
 struct FF {
     float hi, lo;
@@ -87,12 +93,28 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
     constexpr int NL = 32 * W;
     constexpr int kLevels = W == 1 ? 5 : W == 2 ? 6 : 7;
     static_assert(W == 1 || W == 2 || W == 4, "1, 2 or 4 warps per PDE");
-    extern __shared__ float tab[];  // [M][kF][NL], then the exchange area (W > 1)
+    // [M][kF][NL] per-lane fields, then (uniform) [M][5][2] shared factors, then the
+    // exchange area (W > 1)
+    extern __shared__ float tab[];
     const int k = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int K = threadIdx.x;  // lane of the PDE group
-    auto T = [&](int i, int f) -> float& { return tab[(i * kF + f) * NL + K]; };
+    constexpr int kTabFloats = M * kF * NL + (kUni ? M * kSharedFields * 2 : 0);
+    // this lane's copy of the shared factors: +1 for the last lane only, computed
+    // arithmetically ((K + 1) / NL with NL a power of two) so that the loads stay
+    // single loads from one base address
+    float* const shr = tab + M * kF * NL + (K + 1) / NL;
+    // uniform grid: lane 0 writes the group's factors, the last lane its own
+    const bool writer = !kUni || K == 0 || K == NL - 1;
+    auto T = [&](int i, int f) -> float& {
+        if constexpr (kUni) {
+            if (f >= T_PH) return tab[(i * kF + (f - T_PH)) * NL + K];
+            return shr[(i * kSharedFields + f) * 2];
+        } else {
+            return tab[(i * kF + f) * NL + K];
+        }
+    };
     const int j0 = K * M;
-    float2* x_last = reinterpret_cast<float2*>(tab + M * kF * NL);  // [NL] (H, Lo) of each lane's last node
+    float2* x_last = reinterpret_cast<float2*>(tab + kTabFloats);  // [NL] (H, Lo) of each lane's last node
     float2* x_first = x_last + NL;                                  // [NL] of its first node
     float* x_y = reinterpret_cast<float*>(x_first + NL);            // [NL]
     float* x_p0 = x_y + NL;                                         // [NL] x 2: reduction buffers
@@ -200,9 +222,11 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
                     if (!(d != 0.) || !isfinite(d)) st = st == KWG_STATUS_OK ? KWG_STATUS_SOLVER : st;
                     const double idd = 1. / d;
                     const double u = bu * idd;
-                    T(i, T_L) = (float)l;
-                    T(i, T_ID) = (float)idd;
-                    T(i, T_U) = (float)u;
+                    if (writer) {
+                        T(i, T_L) = (float)l;
+                        T(i, T_ID) = (float)idd;
+                        T(i, T_U) = (float)u;
+                    }
                     // spike ends: L = B_I^-1 (bl_1 e_1), R = B_I^-1 (bu_{M-1} e_{M-1}).
                     // L_1 = bl_1 (B_I^-1)_11 = bl_1 sum_k prod_{i<k}(-u_i) / d_k prod_{2<=i<=k}(-l_i)
                     if (i == 1) {
@@ -233,7 +257,7 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
             bl_first_f = bl_first;
         }
         // full spike arrays for the per-step correction, in FP32 from the stored LU
-        {
+        if (writer) {
             float f = (float)bl_first_f;
 #pragma unroll 1
             for (int i = 1; i < M; ++i) {
@@ -331,6 +355,12 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
             __syncthreads();
         }
         const bool run = st == KWG_STATUS_OK;
+        if constexpr (kUni) {  // the shared factors written by lane 0 and the last lane
+            if constexpr (W == 1)
+                __syncwarp();
+            else
+                __syncthreads();
+        }
         float H[M], Lo[M];  // V as float-float pairs, starting at the payoff
 #pragma unroll
         for (int i = 0; i < M; ++i) {
@@ -519,7 +549,8 @@ int& per_sm_fp32()
 template <int M, bool kUni, int W>
 constexpr size_t fp32_smem()
 {
-    return (size_t)M * f32_fields<kUni>() * 32 * W * sizeof(float) + f32_xchg_bytes<W>();
+    return ((size_t)M * f32_fields<kUni>() * 32 * W + (kUni ? (size_t)M * kSharedFields * 2 : 0)) * sizeof(float) +
+           f32_xchg_bytes<W>();
 }
 
 template <int M, bool kUni, int W>
