@@ -30,17 +30,40 @@ constexpr unsigned kFull64 = 0xffffffffu;
 constexpr int kP64Fields = 6;
 // table fields per node, layout [node-in-lane][field][lane]
 enum { Q_L = 0, Q_U, Q_ID, Q_SL, Q_SR, Q_P };
+// kShared (uniform grid, x_dim == 32 M): every interior row of T is the same (built
+// from the exact spacing hx), so every lane but the last -- whose block holds the
+// boundary row -- has bit-identical factors and spikes.  Those 5 fields are then
+// kept once per PDE plus once for the last lane, [node][field][2], read as
+// broadcasts; only the payoff stays per lane ([node][lane]).
+constexpr int kP64Shared = 5;
+
+template <int M, bool kShared>
+constexpr size_t pcr64_smem()
+{
+    return (kShared ? (size_t)M * 32 + (size_t)M * kP64Shared * 2 : (size_t)M * kP64Fields * 32) * sizeof(double);
+}
 
 }  // namespace
 
-template <int M, bool kHalf>
+template <int M, bool kHalf, bool kShared>
 __global__ void __launch_bounds__(32) fd1d_solve_fp64_pcr(const PdeBatch b, Fd1dShape sh, double* __restrict__ vout,
                                                           int32_t* __restrict__ pde_status,
                                                           int* __restrict__ counters)
 {
-    extern __shared__ double qtab[];  // [M][kP64Fields][32]
+    extern __shared__ double qtab[];  // [M][kP64Fields][32], or (kShared) [M][32] + [M][5][2]
     const int k = threadIdx.x & 31;
-    auto Q = [&](int i, int f) -> double& { return qtab[(i * kP64Fields + f) * 32 + k]; };
+    // this lane's copy of the shared factors: +1 for lane 31 only (arithmetic, so
+    // that each access stays one load from one base address)
+    double* const qshr = qtab + M * 32 + (k + 1) / 32;
+    const bool writer = !kShared || k == 0 || k == 31;
+    auto Q = [&](int i, int f) -> double& {
+        if constexpr (kShared) {
+            if (f == Q_P) return qtab[i * 32 + k];
+            return qshr[(i * kP64Shared + f) * 2];
+        } else {
+            return qtab[(i * kP64Fields + f) * 32 + k];
+        }
+    };
     const int j0 = k * M;
 
     for (;;) {
@@ -94,9 +117,11 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64_pcr(const PdeBatch b, Fd1d
                     const double l = (i == 1) ? 0. : tl / d_prev;
                     const double d = (i == 1) ? tm : tm - l * tu_prev;
                     if (!(d != 0.) || !isfinite(d)) st = st == KWG_STATUS_OK ? KWG_STATUS_SOLVER : st;
-                    Q(i, Q_L) = l;
-                    Q(i, Q_ID) = 1. / d;
-                    Q(i, Q_U) = tu / d;  // U = diag(d) (1 + u shift): y_i = f_i/d_i - u_i y_{i+1}
+                    if (writer) {
+                        Q(i, Q_L) = l;
+                        Q(i, Q_ID) = 1. / d;
+                        Q(i, Q_U) = tu / d;  // U = diag(d) (1 + u shift): y_i = f_i/d_i - u_i y_{i+1}
+                    }
                     if (i == 1) tl_first = tl;
                     if (i == M - 1) tu_last = tu;
                     d_prev = d;
@@ -107,7 +132,7 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64_pcr(const PdeBatch b, Fd1d
             }
         }
         // spikes L = T_I^-1 (tl_first e_1), R = T_I^-1 (tu_last e_{M-1})
-        {
+        if (writer) {
             double f = tl_first;
 #pragma unroll 1
             for (int i = 1; i < M; ++i) {
@@ -129,6 +154,7 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64_pcr(const PdeBatch b, Fd1d
                 Q(i, Q_SR) = rn;
             }
         }
+        if constexpr (kShared) __syncwarp();  // lane 0's and lane 31's factors
         // separator system and its cyclic-reduction multipliers
         double ka[5], kc[5], ib;
         {
@@ -223,31 +249,42 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64_pcr(const PdeBatch b, Fd1d
 
 namespace {
 
-template <int M>
+// Resident blocks per SM of fd1d_solve_fp64_pcr<M, *, kShared>, set by fd1d_pcr64_prepare.
+template <int M, bool kShared>
 int& per_sm_pcr64()
 {
     static int v = 1;
     return v;
 }
 
-template <int M>
-void prepare_pcr64()
+template <int M, bool kShared>
+void prepare_pcr64_variant()
 {
-    const size_t smem = (size_t)M * kP64Fields * 32 * sizeof(double);
-    cudaFuncSetAttribute(fd1d_solve_fp64_pcr<M, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(fd1d_solve_fp64_pcr<M, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = pcr64_smem<M, kShared>();
+    cudaFuncSetAttribute(fd1d_solve_fp64_pcr<M, true, kShared>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    cudaFuncSetAttribute(fd1d_solve_fp64_pcr<M, false, kShared>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fd1d_solve_fp64_pcr<M, true>, 32, smem);
-    per_sm_pcr64<M>() = per_sm < 1 ? 1 : per_sm;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fd1d_solve_fp64_pcr<M, true, kShared>, 32, smem);
+    per_sm_pcr64<M, kShared>() = per_sm < 1 ? 1 : per_sm;
 }
 
 template <int M>
-int launch_pcr64(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* vout, int32_t* pde_status,
-                 int* counters, double* prices, int32_t* status, int sms, cudaStream_t stream, const SolveEvents* ev)
+void prepare_pcr64()
 {
-    const size_t smem = (size_t)M * kP64Fields * 32 * sizeof(double);
-    auto kern = sh.c == 1. ? fd1d_solve_fp64_pcr<M, true> : fd1d_solve_fp64_pcr<M, false>;
-    const int per_sm = per_sm_pcr64<M>();
+    prepare_pcr64_variant<M, false>();
+    prepare_pcr64_variant<M, true>();
+}
+
+template <int M, bool kShared>
+int launch_pcr64_variant(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* vout,
+                         int32_t* pde_status, int* counters, double* prices, int32_t* status, int sms,
+                         cudaStream_t stream, const SolveEvents* ev)
+{
+    const size_t smem = pcr64_smem<M, kShared>();
+    auto kern = sh.c == 1. ? fd1d_solve_fp64_pcr<M, true, kShared> : fd1d_solve_fp64_pcr<M, false, kShared>;
+    const int per_sm = per_sm_pcr64<M, kShared>();
     const int blocks = b.m < sms * per_sm ? b.m : sms * per_sm;
     cudaMemsetAsync(counters, 0, 4 * sizeof(int), stream);
     if (ev) cudaEventRecord(ev->start, stream);
@@ -259,6 +296,17 @@ int launch_pcr64(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, do
         ++launches;
     }
     return launches;
+}
+
+// Shared factor tables on uniform grids whose PDEs fill every lane (x_dim == 32 M).
+template <int M>
+int launch_pcr64(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh, double* vout, int32_t* pde_status,
+                 int* counters, double* prices, int32_t* status, int sms, cudaStream_t stream, const SolveEvents* ev)
+{
+    const bool full = sh.pde_x ? sh.full_lanes : sh.x_dim == 32 * M;
+    if (sh.uniform && full)
+        return launch_pcr64_variant<M, true>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
+    return launch_pcr64_variant<M, false>(b, a, sh, vout, pde_status, counters, prices, status, sms, stream, ev);
 }
 
 }  // namespace

@@ -284,6 +284,30 @@ def test_device_dedup_matches_host_dedup(ctx, precision, solver):
     assert np.isnan(got[~ok]).all()
 
 
+@pytest.mark.parametrize("x_dim,short", [(256, 250), (1024, 1000)])
+def test_pcr_shared_tables_are_exact(ctx, x_dim, short):
+    """On a uniform grid whose PDEs fill every lane (x_dim = 32 M) the FP64 PCR solver
+    keeps one copy of the interior factors and spikes per PDE.  The rows are built
+    from the exact spacing, so the copy is bit-identical to every lane's own: prices
+    equal bit for bit those of the per-lane tables, which an uneven batch forces when
+    its bucket also holds one shorter grid."""
+    import kwg
+    import portfolio
+
+    o = portfolio.american_portfolio(200, seed=12)
+    rc, shared, st = ctx.fd1d_price(o, kwg.params(t_dim=64, x_dim=x_dim, scale=5.0, density=math.inf, solver=2))
+    assert rc == 0, ctx.last_error()
+    oo = np.concatenate([o, portfolio.american_portfolio(1, seed=99)])
+    xd = np.array([x_dim] * len(o) + [short], np.int32)
+    td = np.full(len(oo), 64, np.int32)
+    rc, per_lane, st2 = ctx.fd1d_price_uneven(oo, xd, td, kwg.params(scale=5.0, density=math.inf, solver=2))
+    assert rc == 0, ctx.last_error()
+    assert np.array_equal(st, st2[: len(o)])
+    ok = st == 0
+    assert ok.sum() > 150
+    assert np.array_equal(shared[ok], per_lane[: len(o)][ok])
+
+
 def test_million_option_batch(ctx):
     """Maximum-size batch through both entry points: 2^20 options (a quarter of
     them repeated keys), 64 x 64 grid.  Every option prices, the host call and the
