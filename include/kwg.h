@@ -83,8 +83,8 @@ typedef struct kwg_fd1d_params {
     int32_t block_warps;  /* FP64 streaming solver: warps (32 options each) per thread
                              block, 1, 2 or 4; 0 (default) = tuned or 1 */
     int32_t option_warps; /* warp-per-PDE FP32 solver: warps (32 threads each) per
-                             option, 1, 2 or 4 (grids of more than 1024 nodes at least
-                             2; at least 2 nodes per lane); 0 (default) = tuned or 1 */
+                             option, 1, 2, 4 or 8 (grids of more than 1024 nodes at
+                             least 2; at least 2 nodes per lane); 0 (default) = tuned or 1 */
     int32_t sm_blocks;    /* FP64 streaming solver: resident blocks per SM, 0 (default) =
                              tuned or as many as fit (two 4-warp blocks).  With
                              block_warps 4 and sm_blocks 1 each of an SM's four warp
@@ -186,11 +186,12 @@ typedef struct kwg_tuning {
                              use fewer: at least 2 nodes per lane, and at least 2 warps
                              for grids of more than 1024 nodes) */
     double spread_ms;     /* streaming FP64 solver, 4 warps per block, one block per SM */
+    double fp32_8w_ms;    /* FP32 solver with 8 warps per option (same caveat) */
 } kwg_tuning;
 
 /* Autotuner (no counterpart in the reference): on a synthetic batch of m options of
  * p's shape and precision, times options-per-block (1, 2, 4 warps of 32 per block, and
- * one 4-warp block per SM) and Thomas vs PCR for FP64, threads-per-option (1, 2 or 4 warps) for FP32, and records
+ * one 4-warp block per SM) and Thomas vs PCR for FP64, threads-per-option (1, 2, 4 or 8 warps) for FP32, and records
  * the fastest for later calls of that shape whose p leaves the choices at 0 / AUTO.
  * `out` may be NULL. */
 int kwg_autotune_ex(kwg_ctx* ctx, const kwg_fd1d_params* p, size_t m, kwg_tuning* out);

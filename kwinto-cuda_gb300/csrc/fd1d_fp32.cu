@@ -1,5 +1,5 @@
-// fd1d_fp32.cu -- FP32 stepping with FP64-accurate state: one, two or four warps per
-// PDE (tuned; at least two for grids of 1025..2048 nodes), the whole PDE on chip (state in
+// fd1d_fp32.cu -- FP32 stepping with FP64-accurate state: one, two, four or eight warps
+// per PDE (tuned; at least two for grids of 1025..2048 nodes), the whole PDE on chip (state in
 // registers, coefficient tables in shared memory), a partitioned tridiagonal solve
 // with a cyclic reduction of the separator system (warp shuffles; shared memory
 // across the warps of a PDE).
@@ -91,8 +91,8 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
 {
     constexpr int kF = f32_fields<kUni>();
     constexpr int NL = 32 * W;
-    constexpr int kLevels = W == 1 ? 5 : W == 2 ? 6 : 7;
-    static_assert(W == 1 || W == 2 || W == 4, "1, 2 or 4 warps per PDE");
+    constexpr int kLevels = W == 1 ? 5 : W == 2 ? 6 : W == 4 ? 7 : 8;  // log2 of the lanes
+    static_assert(W == 1 || W == 2 || W == 4 || W == 8, "1, 2, 4 or 8 warps per PDE");
     // [M][kF][NL] per-lane fields, then (uniform) [M][5][2] shared factors, then the
     // exchange area (W > 1)
     extern __shared__ float tab[];
@@ -619,6 +619,9 @@ void fd1d_fp32_prepare(int)
     prepare_m<4, 4>();
     prepare_m<8, 4>();
     prepare_m<16, 4>();
+    prepare_m<2, 8>();
+    prepare_m<4, 8>();
+    prepare_m<8, 8>();
 }
 
 int fd1d_fp32_nodes_per_lane(int x_dim)
@@ -636,12 +639,12 @@ int fd1d_fp32_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh
 {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    // W = 1, 2 or 4 warps per PDE (sh.option_warps), each lane owning M = m1 / W nodes,
+    // W = 1, 2, 4 or 8 warps per PDE (sh.option_warps), each lane owning M = m1 / W nodes,
     // m1 the nodes per lane of the one-warp layout; at least 2 nodes per lane, and
     // grids of 1025..2048 nodes take at least two warps
     const int m1 = fd1d_fp32_nodes_per_lane(sh.x_dim);
     if (m1 < 0) return -1;
-    int w = sh.option_warps == 4 ? 4 : sh.option_warps == 2 ? 2 : 1;
+    int w = sh.option_warps == 8 ? 8 : sh.option_warps == 4 ? 4 : sh.option_warps == 2 ? 2 : 1;
     if (m1 == 64 && w < 2) w = 2;
     while (w > 1 && m1 / w < 2) w /= 2;
     const int M = m1 / w;
@@ -661,6 +664,9 @@ int fd1d_fp32_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh
     KWG_FP32_LAUNCH(4, 4);
     KWG_FP32_LAUNCH(8, 4);
     KWG_FP32_LAUNCH(16, 4);
+    KWG_FP32_LAUNCH(2, 8);
+    KWG_FP32_LAUNCH(4, 8);
+    KWG_FP32_LAUNCH(8, 8);
 #undef KWG_FP32_LAUNCH
     return -1;
 }

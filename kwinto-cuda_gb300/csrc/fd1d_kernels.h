@@ -90,10 +90,9 @@ int fd1d_fp64_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh
                      int* counters, double* prices, int32_t* status, int solve_blocks, cudaStream_t stream,
                      const SolveEvents* ev);
 
-// FP32 stepping (one, two or four warps per PDE, on chip; sh.option_warps).  Nodes per
+// FP32 stepping (one, two, four or eight warps per PDE, on chip; sh.option_warps).  Nodes per
 // lane M of the one-warp layout for an x-grid of x_dim nodes (the grid is padded to
-// 32*M with decoupled identity rows; two or four warps take M/2 or M/4 each); -1 if
-// x_dim > 2048.
+// 32*M with decoupled identity rows; W warps take M/W each); -1 if x_dim > 2048.
 // The work buffer holds the final V of every PDE, [m][x_dim] doubles.
 int fd1d_fp32_nodes_per_lane(int x_dim);
 size_t fd1d_fp32_work_bytes(int m, int x_dim);

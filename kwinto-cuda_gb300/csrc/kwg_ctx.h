@@ -131,8 +131,9 @@ inline int check_params(kwg_ctx* ctx, const kwg_fd1d_params* p)
         return set_err(ctx, KWG_ERR_INVALID, "kwg: FP32 stepping supports x_dim <= 2048");
     if (p->block_warps != 0 && p->block_warps != 1 && p->block_warps != 2 && p->block_warps != 4)
         return set_err(ctx, KWG_ERR_INVALID, "kwg: block_warps must be 0, 1, 2 or 4");
-    if (p->option_warps != 0 && p->option_warps != 1 && p->option_warps != 2 && p->option_warps != 4)
-        return set_err(ctx, KWG_ERR_INVALID, "kwg: option_warps must be 0, 1, 2 or 4");
+    if (p->option_warps != 0 && p->option_warps != 1 && p->option_warps != 2 && p->option_warps != 4 &&
+        p->option_warps != 8)
+        return set_err(ctx, KWG_ERR_INVALID, "kwg: option_warps must be 0, 1, 2, 4 or 8");
     if (p->sm_blocks < 0 || p->sm_blocks > 64)
         return set_err(ctx, KWG_ERR_INVALID, "kwg: sm_blocks must be in [0, 64]");
     return KWG_OK;
@@ -166,7 +167,7 @@ inline double time_solve(kwg_ctx* ctx, F&& call)
 // Times every candidate launch shape on fn(params) and returns the fastest: FP64 --
 // the streaming solver with 1, 2, 4 warps per block (as many blocks per SM as fit),
 // with one 4-warp block per SM (one warp per scheduler), and the warp-per-PDE solver
-// (when pcr_ok); FP32 -- 1, 2 and 4 warps per option.
+// (when pcr_ok); FP32 -- 1, 2, 4 and 8 warps per option.
 template <typename F>
 inline kwg_ctx::Tuned tune(kwg_ctx* ctx, const kwg_fd1d_params* p, bool pcr_ok, F&& fn, kwg_tuning* out)
 {
@@ -175,6 +176,7 @@ inline kwg_ctx::Tuned tune(kwg_ctx* ctx, const kwg_fd1d_params* p, bool pcr_ok, 
     r.pcr_ms = -1.;
     for (double& v : r.fp32_ms) v = -1.;
     r.spread_ms = -1.;
+    r.fp32_8w_ms = -1.;
     kwg_fd1d_params q = *p;
     q.strict = 0;
     kwg_ctx::Tuned best;
@@ -209,11 +211,12 @@ inline kwg_ctx::Tuned tune(kwg_ctx* ctx, const kwg_fd1d_params* p, bool pcr_ok, 
             consider(r.pcr_ms, KWG_SOLVER_PCR, 1, 1, 0);
         }
     } else {
-        const int ws[3] = {1, 2, 4};
-        for (int i = 0; i < 3; ++i) {
+        const int ws[4] = {1, 2, 4, 8};
+        for (int i = 0; i < 4; ++i) {
             q.option_warps = ws[i];
-            r.fp32_ms[i] = time_solve(ctx, [&] { return fn(q); });
-            consider(r.fp32_ms[i], KWG_SOLVER_PCR, 1, ws[i], 0);
+            double& ms = i < 3 ? r.fp32_ms[i] : r.fp32_8w_ms;
+            ms = time_solve(ctx, [&] { return fn(q); });
+            consider(ms, KWG_SOLVER_PCR, 1, ws[i], 0);
         }
     }
     r.solver = best.solver;

@@ -86,6 +86,7 @@ class Tuning(ctypes.Structure):
         ("pcr_ms", ctypes.c_double),
         ("fp32_ms", ctypes.c_double * 3),
         ("spread_ms", ctypes.c_double),
+        ("fp32_8w_ms", ctypes.c_double),
     ]
 
     def as_dict(self) -> dict:
@@ -94,7 +95,8 @@ class Tuning(ctypes.Structure):
                 "thomas_ms_by_block_warps": {1: self.thomas_ms[0], 2: self.thomas_ms[1], 4: self.thomas_ms[2]},
                 "thomas_ms_one_4warp_block_per_sm": self.spread_ms,
                 "pcr_ms": self.pcr_ms,
-                "fp32_ms_by_option_warps": {1: self.fp32_ms[0], 2: self.fp32_ms[1], 4: self.fp32_ms[2]}}
+                "fp32_ms_by_option_warps": {1: self.fp32_ms[0], 2: self.fp32_ms[1], 4: self.fp32_ms[2],
+                                            8: self.fp32_8w_ms}}
 
 
 _lib = None

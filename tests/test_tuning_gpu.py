@@ -1,6 +1,6 @@
 """Launch-shape knobs and the autotuner: options per block of the streaming FP64
 solver (1, 2, 4 warps of 32 options) and its resident blocks per SM, threads per
-option of the FP32 solver (1, 2 or 4 warps), Thomas vs PCR.  Every shape must price identically (FP64 streaming: bit for
+option of the FP32 solver (1, 2, 4 or 8 warps), Thomas vs PCR.  Every shape must price identically (FP64 streaming: bit for
 bit, lanes do not depend on their neighbours) or within the FP32 bar."""
 import math
 
@@ -30,12 +30,13 @@ def test_block_warps_are_bit_identical(ctx, bw, sm):
     assert np.array_equal(price(ctx, o, block_warps=bw, sm_blocks=sm, **kw), price(ctx, o, block_warps=1, **kw))
 
 
-@pytest.mark.parametrize("warps", [2, 4])
+@pytest.mark.parametrize("warps", [2, 4, 8])
 @pytest.mark.parametrize("x_dim", [128, 256, 512, 1000, 1024, 2048])
 def test_fp32_multi_warp_options(ctx, x_dim, warps):
-    """Two or four warps per option (64 or 128 lanes, 6 or 7 reduction levels through
-    shared memory; fewer warps where a lane would get under 2 nodes) against the FP64
-    oracle, on uniform grids (the 7-field tables) and the padded 1000-node grid."""
+    """Two, four or eight warps per option (64, 128 or 256 lanes, 6 to 8 reduction
+    levels through shared memory; fewer warps where a lane would get under 2 nodes)
+    against the FP64 oracle, on uniform grids (shared factor tables) and the padded
+    1000-node grid."""
     import kwg
     import kwor
     import portfolio
@@ -74,7 +75,7 @@ def test_autotune_records_and_applies_the_choice(ctx):
     assert np.array_equal(auto, explicit)
     # FP32: threads per option
     t32 = ctx.autotune_ex(kwg.params(t_dim=64, x_dim=512, scale=5.0, density=math.inf, precision=kwg.FP32), 2048)
-    assert t32.option_warps in (1, 2, 4) and min(t32.fp32_ms) > 0
+    assert t32.option_warps in (1, 2, 4, 8) and min(t32.fp32_ms) > 0 and t32.fp32_8w_ms > 0
 
 
 def test_autotune_uneven(ctx):
