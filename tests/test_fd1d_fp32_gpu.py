@@ -58,14 +58,16 @@ def test_portfolio_qdfp(ctx):
     assert np.max(np.abs(p - g["quantlib"])) <= 0.005
 
 
+@pytest.mark.parametrize("warps", [0, 8])
 @pytest.mark.parametrize("name,kw", [("default", {}), ("x3_t2", dict(x_dim=3, t_dim=2)),
                                      ("x7_t5", dict(x_dim=7, t_dim=5)),
                                      ("x64_t33", dict(x_dim=64, t_dim=33, scale=5.0))])
-def test_edge_grids(ctx, name, kw):
+def test_edge_grids(ctx, name, kw, warps):
     """Tiny and non-power-of-two grids (padded with decoupled rows), Europeans,
-    calls, duplicates."""
+    calls, duplicates; with the default launch and with eight warps per PDE asked
+    for (reduced to what the grid allows: at least 2 nodes per lane)."""
     g = golden("edge.npz")
-    p, st = price32(ctx, g["opts"], **kw)
+    p, st = price32(ctx, g["opts"], option_warps=warps, **kw)
     assert (st == 0).all()
     want = g[f"ref_{name}"]
     # a 3-node grid over +-50 sigma sqrt(T) prices some options in the tens of
@@ -73,8 +75,9 @@ def test_edge_grids(ctx, name, kw):
     assert (np.abs(p - want) <= np.maximum(ABS_TOL, 2e-7 * np.abs(want))).all()
 
 
+@pytest.mark.parametrize("warps", [0, 8])
 @pytest.mark.parametrize("x_dim,t_dim", [(100, 50), (300, 120), (1000, 700), (1500, 1200), (1000, 64), (1500, 40)])
-def test_non_power_of_two_grids(ctx, x_dim, t_dim):
+def test_non_power_of_two_grids(ctx, x_dim, t_dim, warps):
     """Grids padded to 32*2^k nodes with decoupled identity rows.  The last two have
     few, long time steps: lambda = theta dt sigma^2 / (2 dx^2) reaches ~1e3 near the
     strike on the sinh grid, where the separator system nearly cancels -- its
@@ -82,7 +85,7 @@ def test_non_power_of_two_grids(ctx, x_dim, t_dim):
     import portfolio
 
     o = portfolio.american_portfolio(40, seed=21)
-    p, st = price32(ctx, o, t_dim=t_dim, x_dim=x_dim, scale=5.0, density=0.25)
+    p, st = price32(ctx, o, t_dim=t_dim, x_dim=x_dim, scale=5.0, density=0.25, option_warps=warps)
     want = oracle(o, t_dim=t_dim, x_dim=x_dim, scale=5.0, density=0.25)
     assert (st == 0).all() and np.max(np.abs(p - want)) <= ABS_TOL
 
