@@ -2,8 +2,8 @@
  * fd1d_oracle.c -- CPU restatement of the reference FD1D American-option pricer.
  *
  * TEST INFRASTRUCTURE ONLY.  This file is the oracle: the parity tests, the smoke
- * check and the CPU-baseline leg of the benchmark call it as the checker.  The
- * product path (libkwg.so) never links, loads or calls it.
+ * check and the CPU-baseline leg of the benchmark compare against it.  The product
+ * path (libkwg.so) never links, loads or calls it.
  *
  * It restates, in plain C and in the same floating-point evaluation order, the
  * algorithm of gituliar/kwinto-cuda:

@@ -1,4 +1,4 @@
-"""ctypes wrappers of the two CPU checkers.  TEST INFRASTRUCTURE ONLY.
+"""ctypes wrappers of the two CPU oracles.  TEST INFRASTRUCTURE ONLY.
 
   oracle/libkwor.so        C restatement of the reference FD1D pricer (fd1d_oracle.c)
   oracle/_ref/libkwref.so  the reference's own sources + ref_harness.cpp (built only
