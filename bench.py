@@ -242,7 +242,7 @@ SURROGATE_CHECK = 32768  # options of the batch re-priced with FD64 for the erro
 
 
 def surrogate_variant(args, ctx, rank, ws, fd32_rate, barrier, max_over_ranks):
-    """Config 5: fresh options through kwg_surrogate_price (host arrays in and out: the
+    """1M fresh options through kwg_surrogate_price (host arrays in and out: the
     network inside its training box, FD32 at 1024 x 1024 for out-of-box options and a
     1% seeded audit).  Error vs FD64 (1024 x 1024) on a seeded subsample of the batch."""
     import torch
