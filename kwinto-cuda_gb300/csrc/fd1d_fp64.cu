@@ -291,6 +291,8 @@ constexpr uint32_t kStageBytes = kStageCoef + kStageP + kStageS;
 // one warp's ring and mbarriers, rounded so the next warp's stages stay aligned
 constexpr size_t kSolveSmem = (kRing * kStageBytes + kRing * sizeof(uint64_t) + 127) / 128 * 128;
 constexpr int kMaxBlockWarps = 4;
+// share of the L2 given to the state lines at the sweep ends (evict-last)
+constexpr double kKeepShare = 0.5;
 
 struct Ring {
     unsigned char* stage;  // kRing * kStageBytes
@@ -323,9 +325,18 @@ struct Ranges {
     int lo, hi, zlo, zhi;
 };
 
+// L2 policies of a sweep: the state stores of its last keep_n nodes -- the first the
+// next sweep, which runs the other way, reads back -- are kept in L2 (evict-last);
+// everything else streams (evict-first).  keep_n == 0: no preference.
+struct Hints {
+    uint64_t keep, stream;
+    int keep_n;
+};
+
 // Issues stage visit q covering sweep stage g of this tile.
 template <bool kUp>
-__device__ __forceinline__ void issue(const Ring& r, uint32_t q, const TileView& tv, int g, int N, const Ranges& rg)
+__device__ __forceinline__ void issue(const Ring& r, uint32_t q, const TileView& tv, int g, int N, const Ranges& rg,
+                                      uint64_t pol)
 {
     int first, count;
     stage_nodes<kUp>(g, N, first, count);
@@ -336,9 +347,9 @@ __device__ __forceinline__ void issue(const Ring& r, uint32_t q, const TileView&
     const uint32_t cb = compact ? 0u : count * kNodeCoefBytes;
     const uint32_t pb = pfree ? 0u : count * kNodePBytes, sb = count * kNodeSBytes;
     mbar_arrive_expect_tx(&r.bar[s], cb + pb + sb);
-    if (!compact) bulk_g2s(st, (kUp ? tv.cu : tv.cd) + (size_t)first * kCoef * kTile, cb, &r.bar[s]);
-    if (!pfree) bulk_g2s(st + kStageCoef, tv.p + (size_t)first * kTile, pb, &r.bar[s]);
-    bulk_g2s(st + kStageCoef + kStageP, tv.s + (size_t)first * kTile * 2, sb, &r.bar[s]);
+    if (!compact) bulk_g2s_hint(st, (kUp ? tv.cu : tv.cd) + (size_t)first * kCoef * kTile, cb, &r.bar[s], pol);
+    if (!pfree) bulk_g2s_hint(st + kStageCoef, tv.p + (size_t)first * kTile, pb, &r.bar[s], pol);
+    bulk_g2s_hint(st + kStageCoef + kStageP, tv.s + (size_t)first * kTile * 2, sb, &r.bar[s], pol);
 }
 
 // Bounded wait for stage visits [from, to) after a timeout: lets copies in flight
@@ -358,7 +369,7 @@ template <bool kUp, bool kHalf, bool kCompact>
 __device__ __forceinline__ void stage_body(const Ring& ring, uint32_t v, const TileView& tv, int g, int ng, int N,
                                            const Ranges& rg, int first, bool pfree, const unsigned char* st, int lane,
                                            double ca, double cb, double cs, double c, bool amer, bool active,
-                                           double2* sout, double& yh, double& f)
+                                           double2* sout, const Hints& hz, double& yh, double& f)
 {
     const double* sc_ = reinterpret_cast<const double*>(st) + lane;
     const double* sp_ = reinterpret_cast<const double*>(st + kStageCoef) + lane;
@@ -376,7 +387,7 @@ __device__ __forceinline__ void stage_body(const Ring& ring, uint32_t v, const T
         rs[k] = kCompact ? cs : sc_[(idx * kCoef + 2) * kTile];
     }
     __syncwarp();  // the slot fully read before it is refilled
-    if (lane == 0 && g + kRing < ng) issue<kUp>(ring, v + kRing, tv, g + kRing, N, rg);
+    if (lane == 0 && g + kRing < ng) issue<kUp>(ring, v + kRing, tv, g + kRing, N, rg, hz.stream);
 #pragma unroll
     for (int k = 0; k < kGroup; ++k) {
         const int j = kUp ? first + k : first + kGroup - 1 - k;
@@ -384,7 +395,9 @@ __device__ __forceinline__ void stage_body(const Ring& ring, uint32_t v, const T
         double vn = kHalf ? fma(rs[k], yh, -rv[k]) : fma(rs[k], yh, -c * rv[k]);
         if (amer && j < N - 1) vn = max_floor(vn, rp[k]);
         f = fma(-rb[k], f, vn);
-        if (active) sout[(size_t)j * kTile] = make_double2(vn, f);
+        if (active)
+            st_global_f64x2_hint(reinterpret_cast<double*>(sout + (size_t)j * kTile), vn, f,
+                                 (kUp ? j >= N - hz.keep_n : j < hz.keep_n) ? hz.keep : hz.stream);
     }
 }
 
@@ -394,7 +407,8 @@ __device__ __forceinline__ void stage_body(const Ring& ring, uint32_t v, const T
 template <bool kUp, bool kHalf>
 __device__ __forceinline__ void tail_stage(int first, int count, bool compact, bool pfree, const unsigned char* st,
                                            int lane, double ca, double cb, double cs, double c, bool amer,
-                                           bool active, int N, double2* sout, double& yh, double& f)
+                                           bool active, int N, double2* sout, const Hints& hz, double& yh,
+                                           double& f)
 {
     const double* sc_ = reinterpret_cast<const double*>(st) + lane;
     const double* sp_ = reinterpret_cast<const double*>(st + kStageCoef) + lane;
@@ -411,7 +425,9 @@ __device__ __forceinline__ void tail_stage(int first, int count, bool compact, b
         double vn = kHalf ? fma(sg, yh, -sv.x) : fma(sg, yh, -c * sv.x);
         if (amer && j < N - 1) vn = max_floor(vn, pfree ? 0. : sp_[idx * kTile]);
         f = fma(-bb, f, vn);
-        if (active) sout[(size_t)j * kTile] = make_double2(vn, f);
+        if (active)
+            st_global_f64x2_hint(reinterpret_cast<double*>(sout + (size_t)j * kTile), vn, f,
+                                 (kUp ? j >= N - hz.keep_n : j < hz.keep_n) ? hz.keep : hz.stream);
     }
 }
 
@@ -419,7 +435,7 @@ __device__ __forceinline__ void tail_stage(int first, int count, bool compact, b
 template <bool kUp, bool kHalf>
 __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileView& tv, int lane, int N,
                                       const Ranges& rg, const double* cst, double c, bool amer, bool active,
-                                      int* err)
+                                      const Hints& hz, int* err)
 {
     const int ng = (N + kGroup - 1) / kGroup;
     const int pre = ng < kRing ? ng : kRing;
@@ -427,7 +443,7 @@ __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileVi
     fence_proxy_async_global();
     __syncwarp();
     if (lane == 0)
-        for (int g = 0; g < pre; ++g) issue<kUp>(ring, q + g, tv, g, N, rg);
+        for (int g = 0; g < pre; ++g) issue<kUp>(ring, q + g, tv, g, N, rg, hz.stream);
     // middle-region constants: UP uses (nh, l, 1/e), DOWN (uh, m, 1/d)
     const double ca = kUp ? cst[0] : cst[3], cb = kUp ? cst[1] : cst[4], cs = kUp ? cst[2] : cst[5];
     double2* sout = reinterpret_cast<double2*>(tv.s) + lane;
@@ -451,13 +467,13 @@ __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileVi
         const unsigned char* st = ring.stage + (size_t)s * kStageBytes;
         if (count == kGroup && compact)
             stage_body<kUp, kHalf, true>(ring, v, tv, g, ng, N, rg, first, pfree, st, lane, ca, cb, cs, c, amer,
-                                         active, sout, yh, f);
+                                         active, sout, hz, yh, f);
         else if (count == kGroup)
             stage_body<kUp, kHalf, false>(ring, v, tv, g, ng, N, rg, first, pfree, st, lane, ca, cb, cs, c, amer,
-                                          active, sout, yh, f);
+                                          active, sout, hz, yh, f);
         else
-            tail_stage<kUp, kHalf>(first, count, compact, pfree, st, lane, ca, cb, cs, c, amer, active, N, sout, yh,
-                                   f);
+            tail_stage<kUp, kHalf>(first, count, compact, pfree, st, lane, ca, cb, cs, c, amer, active, N, sout, hz,
+                                   yh, f);
     }
     return true;
 }
@@ -469,7 +485,8 @@ __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileVi
 // independent warps (32 options each; each warp has its own ring); the block size is
 // a tuned launch parameter.  The sweeps stream through a 2-deep
 // ring of 8-node stages in shared memory filled by the TMA engine; V and h|f are
-// written back with ordinary 16-byte stores.  If a ring wait expires,
+// written back with 16-byte stores, L2 evict-last for the last sh.keep_nodes nodes of a
+// sweep (read back first by the next one) and evict-first otherwise.  If a ring wait expires,
 // tile_counter[1] is set, the warp drains its copies in flight and leaves; the
 // interpolation kernel then marks every option with KWG_STATUS_DEVICE_TIMEOUT.
 // tile_counter[2..3] accumulates (64-bit) the bytes the launch reads and writes.
@@ -491,6 +508,10 @@ __global__ void __launch_bounds__(32 * kMaxBlockWarps)
 
     const int ntiles = b.m_pad / kTile;
     const Work wk = work_of(base, b.m_pad, sh.node_lanes);
+    Hints hz;
+    hz.keep = l2_policy_evict_last();
+    hz.stream = sh.keep_nodes > 0 ? l2_policy_evict_first() : l2_policy_evict_normal();
+    hz.keep_n = sh.keep_nodes;
     uint32_t q = 0;  // stage visits consumed so far
     for (;;) {
         int tile = 0;
@@ -537,11 +558,13 @@ __global__ void __launch_bounds__(32 * kMaxBlockWarps)
             const unsigned long long n_dn = (unsigned long long)((t_max - 1) / 2);
             atomicAdd(reinterpret_cast<unsigned long long*>(tile_counter + 2), per_up * n_up + per_dn * n_dn);
         }
+        Hints ht = hz;
+        ht.keep_n = min(hz.keep_n, N / 2);
         for (int pass = 1; pass < t_max; ++pass) {
             const bool act = pass < t_lane;
-            const bool ok = (pass & 1) ? sweep<true, kHalf>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act,
+            const bool ok = (pass & 1) ? sweep<true, kHalf>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act, ht,
                                                             &tile_counter[1])
-                                       : sweep<false, kHalf>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act,
+                                       : sweep<false, kHalf>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act, ht,
                                                              &tile_counter[1]);
             if (!ok) return;
             q += ng;
@@ -601,6 +624,7 @@ namespace {
 constexpr int kMaxDevices = 64;
 struct DeviceFacts {
     int sms = 0;
+    int l2 = 0;  // L2 bytes
     int max_blocks[kMaxBlockWarps + 1] = {};  // FP64 streaming solver: blocks per SM by block size
 };
 DeviceFacts g_facts[kMaxDevices];
@@ -618,6 +642,7 @@ void fd1d_prepare_kernels(int device)
     if (prev != device) cudaSetDevice(device);
     DeviceFacts& f = g_facts[device];
     cudaDeviceGetAttribute(&f.sms, cudaDevAttrMultiProcessorCount, device);
+    cudaDeviceGetAttribute(&f.l2, cudaDevAttrL2CacheSize, device);
     cudaFuncSetAttribute(fd1d_solve_fp64<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(kMaxBlockWarps * kSolveSmem));
     cudaFuncSetAttribute(fd1d_solve_fp64<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -665,6 +690,15 @@ int fd1d_fp64_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh
     cudaMemsetAsync(counters, 0, 4 * sizeof(int), stream);
     if (ev) cudaEventRecord(ev->start, stream);
     const int bw = sh.block_warps == 2 || sh.block_warps == 4 ? sh.block_warps : 1;
+    {
+        // nodes per sweep end kept in L2: a share of the L2 split over the resident warps
+        // (each node is 32 lanes x 16 B of state)
+        int dev = 0;
+        cudaGetDevice(&dev);
+        const long long l2 = dev >= 0 && dev < kMaxDevices ? g_facts[dev].l2 : 0;
+        const long long warps = (long long)solve_blocks * bw;
+        sh.keep_nodes = warps > 0 ? (int)((long long)(kKeepShare * (double)l2) / (warps * kTile * 16)) : 0;
+    }
     if (sh.c == 1.)
         fd1d_solve_fp64<true><<<solve_blocks, 32 * bw, bw * kSolveSmem, stream>>>(b, sh, work, counters);
     else

@@ -63,6 +63,7 @@ struct Fd1dShape {
     int block_warps = 1;
     int option_warps = 1;
     int sm_blocks = 0;  // FP64 streaming solver: resident blocks per SM (0: as many as fit)
+    int keep_nodes = 0;  // FP64 streaming solver: nodes at each sweep's end stored evict-last in L2 (set by the launch)
 };
 
 __host__ __device__ inline int shape_x(const Fd1dShape& sh, int pde) { return sh.pde_x ? sh.pde_x[pde] : sh.x_dim; }
