@@ -299,20 +299,6 @@ struct Ring {
     uint64_t* bar;         // kRing mbarriers
 };
 
-// Nodes of stage number g of a sweep: [first, first + count), ascending in memory.
-template <bool kUp>
-__device__ __forceinline__ void stage_nodes(int g, int N, int& first, int& count)
-{
-    if (kUp) {
-        first = g * kGroup;
-        count = min(kGroup, N - first);
-    } else {
-        const int top = N - 1 - g * kGroup;
-        first = max(top - kGroup + 1, 0);
-        count = top - first + 1;
-    }
-}
-
 // A stage skips the coefficients when all its nodes lie in the middle region, and
 // the payoff when all its nodes lie in the tile's payoff-free run (same test).
 __device__ __forceinline__ bool stage_compact(int first, int count, int lo, int hi)
@@ -333,24 +319,98 @@ struct Hints {
     int keep_n;
 };
 
-// Issues stage visit q covering sweep stage g of this tile.
-template <bool kUp>
-__device__ __forceinline__ void issue(const Ring& r, uint32_t q, const TileView& tv, int g, int N, const Ranges& rg,
-                                      uint64_t pol)
-{
+// Wide stages: in the middle region a stage needs no coefficients, so the same slot
+// holds 2 kGroup nodes -- payoff [0, kWideP), state after it -- instead of kGroup
+// nodes with coefficients [0, kStageCoef), payoff, state.  Half the stage overhead
+// (mbarrier wait, warp sync, refill) per node where most nodes are.
+constexpr int kWide = 2 * kGroup;
+constexpr uint32_t kWideP = kWide * kNodePBytes;  // 4 KB
+static_assert(kWideP + kWide * kNodeSBytes == kStageBytes, "a wide stage fills one slot");
+
+// A stage of a sweep: nodes [first, first + count), ascending in memory.
+struct Stage {
     int first, count;
-    stage_nodes<kUp>(g, N, first, count);
-    const bool compact = stage_compact(first, count, rg.lo, rg.hi);
-    const bool pfree = stage_compact(first, count, rg.zlo, rg.zhi);
+    bool wide;     // kWide middle-region nodes in the wide layout
+    bool compact;  // no coefficients: all nodes in the middle region
+    bool pfree;    // no payoff: all nodes in the payoff-free run
+};
+
+// The stage starting at cursor `cur` (kUp: its lowest node, else its highest).  Wide
+// where kWide nodes from the cursor lie in the middle region; else kGroup nodes, fewer
+// only at the sweep's end.  Producer and consumer walk the same sequence.
+template <bool kUp>
+__device__ __forceinline__ Stage stage_at(int cur, int N, const Ranges& rg)
+{
+    Stage s;
+    if (kUp) {
+        s.wide = cur >= rg.lo && cur + kWide - 1 <= rg.hi;
+        s.first = cur;
+        s.count = s.wide ? kWide : min(kGroup, N - cur);
+    } else {
+        s.wide = cur - kWide + 1 >= rg.lo && cur <= rg.hi;
+        s.count = s.wide ? kWide : min(kGroup, cur + 1);
+        s.first = cur - s.count + 1;
+    }
+    s.compact = s.wide || stage_compact(s.first, s.count, rg.lo, rg.hi);
+    s.pfree = stage_compact(s.first, s.count, rg.zlo, rg.zhi);
+    return s;
+}
+
+template <bool kUp>
+__device__ __forceinline__ int sweep_first(int N)
+{
+    return kUp ? 0 : N - 1;
+}
+
+template <bool kUp>
+__device__ __forceinline__ bool sweep_done(int cur, int N)
+{
+    return kUp ? cur >= N : cur < 0;
+}
+
+template <bool kUp>
+__device__ __forceinline__ int stage_after(int cur, const Stage& s)
+{
+    return kUp ? cur + s.count : cur - s.count;
+}
+
+// Bytes a stage moves: its bulk reads plus the state stores.
+__device__ __forceinline__ unsigned long long stage_bytes(const Stage& s)
+{
+    return (unsigned long long)s.count * (2 * kNodeSBytes + (s.pfree ? 0 : kNodePBytes) +
+                                          (s.compact ? 0 : kNodeCoefBytes));
+}
+
+// Issues stage visit q for stage sg of this tile.
+template <bool kUp>
+__device__ __forceinline__ void issue(const Ring& r, uint32_t q, const TileView& tv, const Stage& sg, uint64_t pol)
+{
     const int s = (int)(q % kRing);
     unsigned char* st = r.stage + (size_t)s * kStageBytes;
-    const uint32_t cb = compact ? 0u : count * kNodeCoefBytes;
-    const uint32_t pb = pfree ? 0u : count * kNodePBytes, sb = count * kNodeSBytes;
+    const uint32_t cb = sg.compact ? 0u : sg.count * kNodeCoefBytes;
+    const uint32_t pb = sg.pfree ? 0u : sg.count * kNodePBytes, sb = sg.count * kNodeSBytes;
+    const uint32_t p_off = sg.wide ? 0u : kStageCoef, s_off = sg.wide ? kWideP : kStageCoef + kStageP;
     mbar_arrive_expect_tx(&r.bar[s], cb + pb + sb);
-    if (!compact) bulk_g2s_hint(st, (kUp ? tv.cu : tv.cd) + (size_t)first * kCoef * kTile, cb, &r.bar[s], pol);
-    if (!pfree) bulk_g2s_hint(st + kStageCoef, tv.p + (size_t)first * kTile, pb, &r.bar[s], pol);
-    bulk_g2s_hint(st + kStageCoef + kStageP, tv.s + (size_t)first * kTile * 2, sb, &r.bar[s], pol);
+    if (cb) bulk_g2s_hint(st, (kUp ? tv.cu : tv.cd) + (size_t)sg.first * kCoef * kTile, cb, &r.bar[s], pol);
+    if (pb) bulk_g2s_hint(st + p_off, tv.p + (size_t)sg.first * kTile, pb, &r.bar[s], pol);
+    bulk_g2s_hint(st + s_off, tv.s + (size_t)sg.first * kTile * 2, sb, &r.bar[s], pol);
 }
+
+// The refilling side of a sweep, run by lane 0: the next stage to issue and its
+// visit number.
+template <bool kUp>
+struct Producer {
+    int cur;
+    uint32_t next;
+    __device__ __forceinline__ void refill(const Ring& ring, const TileView& tv, int N, const Ranges& rg, uint64_t pol)
+    {
+        if (sweep_done<kUp>(cur, N)) return;
+        const Stage sg = stage_at<kUp>(cur, N, rg);
+        issue<kUp>(ring, next, tv, sg, pol);
+        cur = stage_after<kUp>(cur, sg);
+        ++next;
+    }
+};
 
 // Bounded wait for stage visits [from, to) after a timeout: lets copies in flight
 // land in shared memory before the block exits.
@@ -359,14 +419,34 @@ __device__ void drain(const Ring& r, uint32_t from, uint32_t to)
     for (uint32_t q = from; q < to; ++q) mbar_wait(&r.bar[q % kRing], (q / kRing) & 1u);
 }
 
-// Loads one full stage (kGroup nodes) into registers, refills its ring slot, and runs
-// the stage's node-steps: the elimination recurrence yh, the new value with the
-// early-exercise floor, the second recurrence f, and the 16-byte (value, f) store of
-// each node.  kCompact: the stage lies in the frozen middle region (coefficients
-// ca, cb, cs).  No per-node guard: the unrolled stage is one block the scheduler
-// interleaves across nodes.
+// The node-steps of one stage held in registers (kG nodes, processing order): the
+// elimination recurrence yh, the new value with the early-exercise floor, the
+// second recurrence f, and the 16-byte (value, f) store of each node.
+template <bool kUp, bool kHalf, int kG>
+__device__ __forceinline__ void stage_steps(const double* ra, const double* rb, const double* rs, const double* rp,
+                                            const double* rv, const double* rw, int first, int N, double c,
+                                            bool amer, bool active, double2* sout, const Hints& hz, double& yh,
+                                            double& f)
+{
+#pragma unroll
+    for (int k = 0; k < kG; ++k) {
+        const int j = kUp ? first + k : first + kG - 1 - k;
+        yh = fma(-ra[k], yh, rw[k]);
+        double vn = kHalf ? fma(rs[k], yh, -rv[k]) : fma(rs[k], yh, -c * rv[k]);
+        if (amer && j < N - 1) vn = max_floor(vn, rp[k]);
+        f = fma(-rb[k], f, vn);
+        if (active)
+            st_global_f64x2_hint(reinterpret_cast<double*>(sout + (size_t)j * kTile), vn, f,
+                                 (kUp ? j >= N - hz.keep_n : j < hz.keep_n) ? hz.keep : hz.stream);
+    }
+}
+
+// One full kGroup-node stage: loads it into registers, lets lane 0 refill the slot,
+// and runs its node-steps.  kCompact: the stage lies in the middle region
+// (coefficients ca, cb, cs).  No per-node guard: the unrolled stage is one block the
+// scheduler interleaves across nodes.
 template <bool kUp, bool kHalf, bool kCompact>
-__device__ __forceinline__ void stage_body(const Ring& ring, uint32_t v, const TileView& tv, int g, int ng, int N,
+__device__ __forceinline__ void stage_body(const Ring& ring, const TileView& tv, Producer<kUp>& prod, int N,
                                            const Ranges& rg, int first, bool pfree, const unsigned char* st, int lane,
                                            double ca, double cb, double cs, double c, bool amer, bool active,
                                            double2* sout, const Hints& hz, double& yh, double& f)
@@ -387,18 +467,34 @@ __device__ __forceinline__ void stage_body(const Ring& ring, uint32_t v, const T
         rs[k] = kCompact ? cs : sc_[(idx * kCoef + 2) * kTile];
     }
     __syncwarp();  // the slot fully read before it is refilled
-    if (lane == 0 && g + kRing < ng) issue<kUp>(ring, v + kRing, tv, g + kRing, N, rg, hz.stream);
+    if (lane == 0) prod.refill(ring, tv, N, rg, hz.stream);
+    stage_steps<kUp, kHalf, kGroup>(ra, rb, rs, rp, rv, rw, first, N, c, amer, active, sout, hz, yh, f);
+}
+
+// One wide stage (kWide middle-region nodes, wide layout).
+template <bool kUp, bool kHalf>
+__device__ __forceinline__ void stage_body_wide(const Ring& ring, const TileView& tv, Producer<kUp>& prod, int N,
+                                                const Ranges& rg, int first, bool pfree, const unsigned char* st,
+                                                int lane, double ca, double cb, double cs, double c, bool amer,
+                                                bool active, double2* sout, const Hints& hz, double& yh, double& f)
+{
+    const double* sp_ = reinterpret_cast<const double*>(st) + lane;
+    const double2* ss_ = reinterpret_cast<const double2*>(st + kWideP) + lane;
+    double ra[kWide], rb[kWide], rs[kWide], rp[kWide], rv[kWide], rw[kWide];
 #pragma unroll
-    for (int k = 0; k < kGroup; ++k) {
-        const int j = kUp ? first + k : first + kGroup - 1 - k;
-        yh = fma(-ra[k], yh, rw[k]);
-        double vn = kHalf ? fma(rs[k], yh, -rv[k]) : fma(rs[k], yh, -c * rv[k]);
-        if (amer && j < N - 1) vn = max_floor(vn, rp[k]);
-        f = fma(-rb[k], f, vn);
-        if (active)
-            st_global_f64x2_hint(reinterpret_cast<double*>(sout + (size_t)j * kTile), vn, f,
-                                 (kUp ? j >= N - hz.keep_n : j < hz.keep_n) ? hz.keep : hz.stream);
+    for (int k = 0; k < kWide; ++k) {
+        const int idx = kUp ? k : kWide - 1 - k;
+        rp[k] = pfree ? 0. : sp_[idx * kTile];
+        const double2 sv = ss_[idx * kTile];
+        rv[k] = sv.x;
+        rw[k] = sv.y;
+        ra[k] = ca;
+        rb[k] = cb;
+        rs[k] = cs;
     }
+    __syncwarp();
+    if (lane == 0) prod.refill(ring, tv, N, rg, hz.stream);
+    stage_steps<kUp, kHalf, kWide>(ra, rb, rs, rp, rv, rw, first, N, c, amer, active, sout, hz, yh, f);
 }
 
 // A sweep's last stage when it holds fewer than kGroup nodes.  It refills no ring
@@ -431,51 +527,52 @@ __device__ __forceinline__ void tail_stage(int first, int count, bool compact, b
     }
 }
 
-// One sweep over this warp's tile.  Returns false on a wait timeout (already drained).
+// One sweep over this warp's tile.  Returns the stage visits it consumed, or -1 on a
+// wait timeout (copies in flight already drained).
 template <bool kUp, bool kHalf>
-__device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileView& tv, int lane, int N,
-                                      const Ranges& rg, const double* cst, double c, bool amer, bool active,
-                                      const Hints& hz, int* err)
+__device__ __forceinline__ int sweep(const Ring& ring, uint32_t q, const TileView& tv, int lane, int N,
+                                     const Ranges& rg, const double* cst, double c, bool amer, bool active,
+                                     const Hints& hz, int* err)
 {
-    const int ng = (N + kGroup - 1) / kGroup;
-    const int pre = ng < kRing ? ng : kRing;
     // the previous sweep's stores must be visible to the bulk-copy engine
     fence_proxy_async_global();
     __syncwarp();
+    Producer<kUp> prod{sweep_first<kUp>(N), q};
     if (lane == 0)
-        for (int g = 0; g < pre; ++g) issue<kUp>(ring, q + g, tv, g, N, rg, hz.stream);
+        for (int i = 0; i < kRing; ++i) prod.refill(ring, tv, N, rg, hz.stream);
     // middle-region constants: UP uses (nh, l, 1/e), DOWN (uh, m, 1/d)
     const double ca = kUp ? cst[0] : cst[3], cb = kUp ? cst[1] : cst[4], cs = kUp ? cst[2] : cst[5];
     double2* sout = reinterpret_cast<double2*>(tv.s) + lane;
     double yh = 0., f = 0.;
-    for (int g = 0; g < ng; ++g) {
-        const uint32_t v = q + g;
+    uint32_t v = q;
+    for (int cur = sweep_first<kUp>(N); !sweep_done<kUp>(cur, N); ++v) {
         const int s = (int)(v % kRing);
         const bool ok = __all_sync(0xffffffffu, mbar_wait(&ring.bar[s], (v / kRing) & 1u));
         if (!ok) {
             if (lane == 0) {
                 atomicExch(err, 1);
-                drain(ring, v, q + min(g + kRing, ng));
+                drain(ring, v, prod.next);
             }
             __syncwarp();
-            return false;
+            return -1;
         }
-        int first, count;
-        stage_nodes<kUp>(g, N, first, count);
-        const bool compact = stage_compact(first, count, rg.lo, rg.hi);
-        const bool pfree = stage_compact(first, count, rg.zlo, rg.zhi);
+        const Stage sg = stage_at<kUp>(cur, N, rg);
         const unsigned char* st = ring.stage + (size_t)s * kStageBytes;
-        if (count == kGroup && compact)
-            stage_body<kUp, kHalf, true>(ring, v, tv, g, ng, N, rg, first, pfree, st, lane, ca, cb, cs, c, amer,
+        if (sg.wide)
+            stage_body_wide<kUp, kHalf>(ring, tv, prod, N, rg, sg.first, sg.pfree, st, lane, ca, cb, cs, c, amer,
+                                        active, sout, hz, yh, f);
+        else if (sg.count == kGroup && sg.compact)
+            stage_body<kUp, kHalf, true>(ring, tv, prod, N, rg, sg.first, sg.pfree, st, lane, ca, cb, cs, c, amer,
                                          active, sout, hz, yh, f);
-        else if (count == kGroup)
-            stage_body<kUp, kHalf, false>(ring, v, tv, g, ng, N, rg, first, pfree, st, lane, ca, cb, cs, c, amer,
+        else if (sg.count == kGroup)
+            stage_body<kUp, kHalf, false>(ring, tv, prod, N, rg, sg.first, sg.pfree, st, lane, ca, cb, cs, c, amer,
                                           active, sout, hz, yh, f);
         else
-            tail_stage<kUp, kHalf>(first, count, compact, pfree, st, lane, ca, cb, cs, c, amer, active, N, sout, hz,
-                                   yh, f);
+            tail_stage<kUp, kHalf>(sg.first, sg.count, sg.compact, sg.pfree, st, lane, ca, cb, cs, c, amer, active,
+                                   N, sout, hz, yh, f);
+        cur = stage_after<kUp>(cur, sg);
     }
-    return true;
+    return (int)(v - q);
 }
 
 }  // namespace
@@ -483,8 +580,9 @@ __device__ __forceinline__ bool sweep(const Ring& ring, uint32_t q, const TileVi
 // Persistent: each warp takes tiles from tile_counter[0] (zeroed by the host before
 // the launch) and runs all tDim-1 steps of its 32 PDEs.  A block holds 1, 2 or 4
 // independent warps (32 options each; each warp has its own ring); the block size is
-// a tuned launch parameter.  The sweeps stream through a 2-deep
-// ring of 8-node stages in shared memory filled by the TMA engine; V and h|f are
+// a tuned launch parameter.  The sweeps stream through a 2-deep ring of stages in
+// shared memory filled by the TMA engine (16 nodes in the middle region, 8 with
+// coefficients elsewhere); V and h|f are
 // written back with 16-byte stores, L2 evict-last for the last sh.keep_nodes nodes of a
 // sweep (read back first by the next one) and evict-first otherwise.  If a ring wait expires,
 // tile_counter[1] is set, the warp drains its copies in flight and leaves; the
@@ -524,7 +622,6 @@ __global__ void __launch_bounds__(32 * kMaxBlockWarps)
         int N;
         long long toff;
         tile_shape(sh, tile, N, toff);
-        const int ng = (N + kGroup - 1) / kGroup;
         const TileView tv = tile_view(wk, toff);
         // every lane steps its own PDE tDim-1 times; the tile runs for its longest
         const int t_lane = shape_t(sh, src);
@@ -543,16 +640,15 @@ __global__ void __launch_bounds__(32 * kMaxBlockWarps)
         if (lane == 0) {
             // bytes this tile moves per sweep: the stages' bulk reads + the state stores
             unsigned long long per_up = 0, per_dn = 0;
-            for (int g = 0; g < ng; ++g) {
-                int first, count;
-                stage_nodes<true>(g, N, first, count);
-                per_up += count * 2 * kNodeSBytes +
-                          (stage_compact(first, count, rg.zlo, rg.zhi) ? 0 : count * kNodePBytes) +
-                          (stage_compact(first, count, lo, hi) ? 0 : count * kNodeCoefBytes);
-                stage_nodes<false>(g, N, first, count);
-                per_dn += count * 2 * kNodeSBytes +
-                          (stage_compact(first, count, rg.zlo, rg.zhi) ? 0 : count * kNodePBytes) +
-                          (stage_compact(first, count, lo, hi) ? 0 : count * kNodeCoefBytes);
+            for (int cur = sweep_first<true>(N); !sweep_done<true>(cur, N);) {
+                const Stage sg = stage_at<true>(cur, N, rg);
+                per_up += stage_bytes(sg);
+                cur = stage_after<true>(cur, sg);
+            }
+            for (int cur = sweep_first<false>(N); !sweep_done<false>(cur, N);) {
+                const Stage sg = stage_at<false>(cur, N, rg);
+                per_dn += stage_bytes(sg);
+                cur = stage_after<false>(cur, sg);
             }
             const unsigned long long n_up = (unsigned long long)(t_max / 2);  // passes 1, 3, 5, ...
             const unsigned long long n_dn = (unsigned long long)((t_max - 1) / 2);
@@ -562,12 +658,12 @@ __global__ void __launch_bounds__(32 * kMaxBlockWarps)
         ht.keep_n = min(hz.keep_n, N / 2);
         for (int pass = 1; pass < t_max; ++pass) {
             const bool act = pass < t_lane;
-            const bool ok = (pass & 1) ? sweep<true, kHalf>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act, ht,
-                                                            &tile_counter[1])
-                                       : sweep<false, kHalf>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act, ht,
-                                                             &tile_counter[1]);
-            if (!ok) return;
-            q += ng;
+            const int used = (pass & 1) ? sweep<true, kHalf>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act, ht,
+                                                             &tile_counter[1])
+                                        : sweep<false, kHalf>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act, ht,
+                                                              &tile_counter[1]);
+            if (used < 0) return;
+            q += (uint32_t)used;
         }
     }
 }
