@@ -37,9 +37,10 @@
 //     CD [node][3][32]  DOWN coefficients (uh, m, 1/d)
 //     P  [node][32]     payoff
 //     S  [node][32][2]  state (V, h|f), one 16-byte load/store per lane
-// A sweep streams them in stages of kGroup consecutive nodes (one mbarrier, one to
-// three bulk copies per stage); in the middle region the coefficients are not read,
-// and where the payoff of every lane of the tile is exactly +0 (the out-of-the-money
+// A sweep streams them in stages of consecutive nodes (one mbarrier, one to three
+// bulk copies per stage): 2 kGroup nodes in the middle region, where the coefficients
+// are not read, kGroup nodes elsewhere.  Where the payoff of every lane of the tile
+// is exactly +0 (the out-of-the-money
 // side of a tile of puts only or calls only; all nodes of European PDEs, which never
 // project) the payoff is not read either: the projection there is max(V, +0).
 #include <atomic>
