@@ -258,6 +258,9 @@ def surrogate_variant(args, ctx, rank, ws, fd32_rate, barrier, max_over_ranks):
     meta = json.loads(str(np.load(SURROGATE_WEIGHTS)["meta"])) if "meta" in np.load(SURROGATE_WEIGHTS) else {}
     opts = portfolio.american_portfolio(n, seed=5005, start=rank * n)
     fd = kwg.params(t_dim=T_DIM, x_dim=X_DIM, scale=SCALE, density=DENSITY, precision=kwg.FP32)
+    # the FD32 launch shape for the audit's batch size (~1 % of the options), as a
+    # caller would tune it once
+    fd_tuning = ctx.autotune_ex(fd, max(1, int(round(n * SURROGATE_AUDIT)))).as_dict()
     for i in range(max(1, args.warmup)):
         prices, route, audit = net.price(ctx, opts, fd, SURROGATE_AUDIT, seed=100 + i)
     barrier()
@@ -298,6 +301,8 @@ def surrogate_variant(args, ctx, rank, ws, fd32_rate, barrier, max_over_ranks):
             "check_sample": len(idx), "p99_abs_err_vs_fd64": float(np.quantile(err, 0.99)),
             "max_abs_err_vs_fd64": float(err.max()), "mean_abs_err_vs_fd64": float(err.mean()),
             "training": meta,
+            "fd32_audit_tuning": {"option_warps": fd_tuning["option_warps"],
+                                  "fp32_ms_by_option_warps": fd_tuning["fp32_ms_by_option_warps"]},
             "workload": "1M fresh options (seeded; S=100, K~U[80,120], vol~U[0.1,0.6], r,q~U[0,0.1], T~U[0.25,2]), 1% audit, FD32 fallback at "
                         "1024x1024; kwg_surrogate_price (host arrays, H2D/D2H inside the timing)"}
 
