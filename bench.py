@@ -526,6 +526,28 @@ def run_ours(args):
             fine["fd64_max_rel_err_vs_oracle"] = float(np.max(np.abs(p64_[idx] - want4) / np.abs(want4)))
             fine["oracle_sample"] = len(idx)
 
+    # ---------------------------------------------------------------- precision, 128 options, 512 x 512 (sinh grid)
+    small = {}
+    if rank == 0:
+        o1 = portfolio.american_portfolio(128, seed=42)
+        kw1 = dict(t_dim=512, x_dim=512, scale=SCALE, density=0.25)
+        rc1, p1_64, s1_64 = ctx.fd1d_price(o1, kwg.params(**kw1))
+        rc2, p1_32, s1_32 = ctx.fd1d_price(o1, kwg.params(precision=kwg.FP32, **kw1))
+        if rc1 != 0 or rc2 != 0:
+            raise RuntimeError(ctx.last_error())
+        ok1 = (s1_64 == 0) & (s1_32 == 0)
+        small = {"options": len(o1), "x_dim": 512, "t_dim": 512, "density": 0.25, "scale": SCALE,
+                 "fd32_max_abs_err_vs_fd64": float(np.abs(p1_32[ok1] - p1_64[ok1]).max()), "failed": int((~ok1).sum())}
+        if not args.no_cpu:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import kwor
+
+            rc3, msg3, want1, _ = kwor.fd1d_price(o1, **kw1)
+            if rc3 != 0:
+                raise RuntimeError(msg3)
+            small["fd64_max_rel_err_vs_oracle"] = float(np.max(np.abs(p1_64[ok1] - want1[ok1]) / np.abs(want1[ok1])))
+            small["fd32_max_abs_err_vs_oracle"] = float(np.abs(p1_32[ok1] - want1[ok1]).max())
+
     tuned = {"fp64": tune64, "fp32": tune32, "uneven_131072": uneven.pop("tuning", None)}
 
     if ws > 1:
@@ -592,6 +614,7 @@ def run_ours(args):
                                             "uniform grids, scale 5; kwg_fd1d_price_uneven (host API, CUDA graph)"),
                      "fd1d_bs_32768x1024": fd1d_bs,
                      "precision_65536x2048": fine,
+                     "precision_128x512": small,
                      "autotune": tuned,
                      "surrogate_1m": surrogate},
     }
