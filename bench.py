@@ -487,7 +487,7 @@ def run_ours(args):
     if not args.no_fine_study:
         o4 = portfolio.american_portfolio(65536, seed=44, start=rank * 65536)
         res4 = {}
-        # threads per option of the FP32 solver on this shape (2 or 4 warps at 2048 nodes)
+        # threads per option of the FP32 solver on this shape (2, 4 or 8 warps at 2048 nodes)
         tune4 = ctx.autotune_ex(kwg.params(t_dim=2048, x_dim=2048, scale=SCALE, density=0.25, precision=kwg.FP32),
                                 len(o4)).as_dict()
         for name, prec in (("fp64", kwg.FP64), ("fp32", kwg.FP32)):

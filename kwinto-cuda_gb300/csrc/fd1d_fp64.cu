@@ -276,14 +276,16 @@ __global__ void __launch_bounds__(128) fd1d_setup_fp64(const PdeBatch b, Fd1dSha
 
 namespace {
 
-// Ring of stages in shared memory; a stage holds kGroup consecutive nodes of one
-// sweep: coefficients [kGroup][3][32], payoff [kGroup][32], state [kGroup][32][2].
-// Stage visits are numbered per warp (q); visit q uses stage q % kRing with
-// mbarrier parity (q / kRing) & 1.
-// 8-node stages, double-buffered: 24 KB per warp keeps >= 7 single-warp blocks per
-// SM (the 1024 tiles of a 32768-option batch in one wave), and measured on the 32768-option
-// 1024 x 1024 batch (launch ms, nodes x ring): 4x4 246, 6x3 236, 7x2 223, 8x2 219, 10x2 401 (6 blocks
-// per SM: a second wave), 2x8 314
+// Ring of stage slots in shared memory; a slot holds kGroup consecutive nodes of one
+// sweep -- coefficients [kGroup][3][32], payoff [kGroup][32], state [kGroup][32][2] --
+// or, in the middle region, 2 kGroup nodes of payoff and state (see kWide below).
+// Stage visits are numbered per warp (q); visit q uses slot q % kRing with mbarrier
+// parity (q / kRing) & 1.
+// 12 KB slots, double-buffered: 24 KB per warp keeps >= 7 single-warp blocks per SM
+// (the 1024 tiles of a 32768-option batch in one wave).  Measured on the 32768-option
+// 1024 x 1024 batch with uniform stages (launch ms, nodes x ring): 4x4 246, 6x3 236,
+// 7x2 223, 8x2 219, 10x2 401 (6 blocks per SM: a second wave), 2x8 314; 16-node
+// middle stages in the same slots then 199.
 constexpr int kRing = 2;
 constexpr uint32_t kStageCoef = kGroup * kNodeCoefBytes;  // 6 KB
 constexpr uint32_t kStageP = kGroup * kNodePBytes;        // 2 KB
