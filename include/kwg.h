@@ -42,7 +42,7 @@ extern "C" {
 
 /* ---- numeric modes ------------------------------------------------------------------- */
 #define KWG_FP64 0 /* all stepping in FP64: parity with the reference to <= 1e-10 relative */
-#define KWG_FP32 1 /* FP32 stepping with FP64-accurate state and residual (see DESIGN) */
+#define KWG_FP32 1 /* FP32 stepping: FP64 setup and interpolation, float-float state and residual */
 
 #define KWG_SOLVER_AUTO 0   /* the autotuned choice for this shape, else a cost model */
 #define KWG_SOLVER_THOMAS 1 /* FP64: thread per option, option-interleaved streaming layout */
@@ -73,9 +73,13 @@ typedef struct kwg_fd1d_params {
                           density -> infinity limit of the sinh grid)        */
     int32_t precision; /* KWG_FP64 (default) or KWG_FP32 */
     int32_t solver;    /* KWG_SOLVER_AUTO (default), _THOMAS or _PCR */
-    int32_t strict;    /* 1: return an error for the first bad option, like the
-                          reference (src/Pricer/kwFd1d.cpp:154-155); 0 (default):
-                          per-option status and NaN, the batch still succeeds */
+    int32_t strict;    /* blocking host calls (kwg_fd1d_price, kwg_fd1d_bs_price,
+                          kwg_fd1d_price_uneven): 1 returns an error for the first
+                          bad option, like the reference
+                          (src/Pricer/kwFd1d.cpp:154-155); 0 (default): per-option
+                          status and NaN, the batch still succeeds.  The
+                          asynchronous device calls reject 1 (KWG_ERR_INVALID): their
+                          caller reads d_status */
     int32_t device_dedup; /* kwg_fd1d_price_device only: 1 deduplicates the options on
                           the device by (t,r,q,z,e,w) like the host path (one stream
                           synchronisation reads the PDE count); 0 (default) solves every
@@ -139,6 +143,7 @@ int kwg_fd1d_bs_price(kwg_ctx* ctx, const kwg_option* opts, size_t n, const kwg_
  * portfolios resident in HBM.  Without p->device_dedup every option is solved as its
  * own PDE; with it the options are deduplicated on the device (hash table on the key
  * of src/Pricer/kwFd1d.cpp:28-65; the call then waits once for the PDE count).
+ * Per-option results are in d_status; p->strict = 1 is rejected (KWG_ERR_INVALID).
  * Replaces kw::Fd1d::solve + kw::Fd1d::value (src/Math/kwFd1d.cpp:11-58, 139-158). */
 int kwg_fd1d_price_device(kwg_ctx* ctx, const kwg_option* d_opts, size_t n,
                           const kwg_fd1d_params* p, double* d_prices, int32_t* d_status,
@@ -148,15 +153,22 @@ int kwg_fd1d_price_device(kwg_ctx* ctx, const kwg_option* d_opts, size_t n,
  * allocate device memory -- for example a pricing step inside a host application
  * whose device memory belongs to another allocator or is held to a fixed budget, or
  * a latency-critical path where cudaMalloc's implicit synchronisation is not allowed.
- * Same computation and results as kwg_fd1d_price_device, but it needs no context and
- * allocates nothing: all scratch is one 64 MiB __device__ array inside the library
- * (about 80 bytes per option and grid node: roughly 800 options at x_dim 1024), held
- * by every GPU that loads the library until the process exits.  Larger batches are
- * rejected with KWG_ERR_INVALID and a message.  The first call on a device looks up
- * the array's address with that device current; make it before any stream capture.
- * Calls share the array: calls that overlap on the GPU race, so serialise them.
- * `stream` is a cudaStream_t (NULL = the legacy default stream); `err` (may be NULL)
- * receives the error message.  Asynchronous like kwg_fd1d_price_device. */
+ * It needs no context and allocates nothing: all scratch is one 64 MiB __device__
+ * array inside the library (about 80 bytes per option and grid node: roughly 800
+ * options at x_dim 1024), held by every GPU that loads the library until the process
+ * exits.  Larger batches are rejected with KWG_ERR_INVALID and a message.
+ * It always runs the streaming Thomas solver (solver AUTO or THOMAS; PCR is
+ * rejected) and solves every option as its own PDE, so its prices are bit-identical
+ * to kwg_fd1d_price_device's with solver THOMAS, and equal to the FP64 parity
+ * tolerance otherwise.  block_warps and sm_blocks apply as there; option_warps (an
+ * FP32 knob) is ignored; strict = 1 and device_dedup = 1 are rejected: read d_status.
+ * Set-up: the first call on a device looks up the array's address with that device
+ * current and caches it with the device's context id; a call that finds another
+ * context (after a device reset) or none current on its thread repeats the look-up.
+ * Make the first call on each device, and from each host thread, before any stream
+ * capture.  Calls share the array: calls that overlap on the GPU race, so serialise
+ * them.  `stream` is a cudaStream_t (NULL = the legacy default stream); `err` (may
+ * be NULL) receives the error message.  Asynchronous like kwg_fd1d_price_device. */
 int kwg_fd1d_price_device_static(const kwg_option* d_opts, size_t n, const kwg_fd1d_params* p,
                                  double* d_prices, int32_t* d_status, void* stream, char* err,
                                  size_t errlen);

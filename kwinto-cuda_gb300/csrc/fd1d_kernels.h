@@ -107,6 +107,15 @@ int fd1d_pcr64_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& s
                       int* counters, double* prices, int32_t* status, int device, cudaStream_t stream,
                       const SolveEvents* ev);
 
+// Device options (56-byte kw::Option records) -> the SoA arrays of a PdeBatch and
+// an AssetBatch, every option its own PDE, the PDEs grouped by exercise / put-call
+// class (European puts, European calls, American puts, American calls) so that the
+// streaming FP64 solver's tiles are homogeneous; the slot order inside a class is
+// arrival order.  counts: 8 ints (per-class counts, cursors), zeroed here on
+// `stream`.  Two launches; returns the first CUDA error.
+cudaError_t unpack_by_class(const void* d_opts, int n, int* counts, double* t, double* z, double* r, double* q,
+                            double* s, double* k, int32_t* pde, int8_t* w, uint8_t* e, cudaStream_t stream);
+
 // Interpolation over a [m][x_dim] array of final values (FP32 and PCR paths).
 __global__ void fd1d_interp_rows(const PdeBatch b, const AssetBatch a, Fd1dShape sh, const double* __restrict__ vrow,
                                  const int32_t* __restrict__ pde_status, double* __restrict__ prices,

@@ -480,6 +480,17 @@ std::vector<kwg_option> tuning_batch(size_t m)
 
 }  // namespace
 
+cudaError_t kwg::unpack_by_class(const void* d_opts, int n, int* counts, double* t, double* z, double* r, double* q,
+                                 double* s, double* k, int32_t* pde, int8_t* w, uint8_t* e, cudaStream_t stream)
+{
+    if (cudaError_t ce = cudaMemsetAsync(counts, 0, 8 * sizeof(int), stream); ce != cudaSuccess) return ce;
+    const kwg_option* o = (const kwg_option*)d_opts;
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    count_classes<<<nb, 256, 0, stream>>>(o, n, counts);
+    unpack_options<<<nb, 256, 0, stream>>>(o, n, counts, counts + 4, t, z, r, q, s, k, pde, w, e);
+    return cudaGetLastError();
+}
+
 
 extern "C" {
 
@@ -653,6 +664,10 @@ int kwg_fd1d_price_device(kwg_ctx* ctx, const kwg_option* d_opts, size_t n, cons
     ctx->err.clear();
     ctx->launches = 0;
     if (int rc = check_params(ctx, p)) return rc;
+    if (p->strict)
+        return set_err(ctx, KWG_ERR_INVALID,
+                       "kwg_fd1d_price_device: strict mode applies to the blocking host calls only; this call is "
+                       "asynchronous, so read d_status (or use kwg_fd1d_price)");
     if (n == 0) return KWG_OK;
     if (!d_opts || !d_prices) return set_err(ctx, KWG_ERR_INVALID, "kwg: null options or prices");
     if (n > (size_t)INT32_MAX / 2) return set_err(ctx, KWG_ERR_INVALID, "kwg: batch too large");
@@ -665,13 +680,10 @@ int kwg_fd1d_price_device(kwg_ctx* ctx, const kwg_option* d_opts, size_t n, cons
     if (int rc = ensure_device(ctx, &ctx->d_io, &ctx->io_bytes, L.total + 8 * sizeof(int))) return rc;
     char* io = (char*)ctx->d_io;
     int* counts = (int*)(io + L.total);  // [4] per-class counts, [4] cursors
-    KWG_CUDA(ctx, cudaMemsetAsync(counts, 0, 8 * sizeof(int), stream));
-    const unsigned nb = (unsigned)((n + 255) / 256);
-    count_classes<<<nb, 256, 0, stream>>>(d_opts, (int)n, counts);
-    unpack_options<<<nb, 256, 0, stream>>>(d_opts, (int)n, counts, counts + 4, (double*)(io + L.t),
-                                           (double*)(io + L.z), (double*)(io + L.r), (double*)(io + L.q),
-                                           (double*)(io + L.s), (double*)(io + L.k), (int32_t*)(io + L.pde),
-                                           (int8_t*)(io + L.w), (uint8_t*)(io + L.e));
+    KWG_CUDA(ctx, kwg::unpack_by_class(d_opts, (int)n, counts, (double*)(io + L.t), (double*)(io + L.z),
+                                       (double*)(io + L.r), (double*)(io + L.q), (double*)(io + L.s),
+                                       (double*)(io + L.k), (int32_t*)(io + L.pde), (int8_t*)(io + L.w),
+                                       (uint8_t*)(io + L.e), stream));
     ctx->launches += 2;
     return run_batch(ctx, io, L, (int)m, (int)n, p, d_prices, d_status, stream);
 }

@@ -4,21 +4,25 @@
 // application whose device memory belongs to another allocator or is held to a
 // fixed budget.  Or it can run on a latency-critical path where cudaMalloc's
 // implicit device synchronisation is not allowed.  kwg_fd1d_price_device_static
-// serves them: it runs the same kernels as kwg_fd1d_price_device, but every
-// byte of scratch (unpacked inputs, per-PDE status, tile queue, node records) lives
+// serves them: it runs the same kernels as kwg_fd1d_price_device with the Thomas
+// solver (class-ordered unpack, setup, streaming solve, interpolation), but every
+// byte of scratch (unpacked inputs, per-PDE status, counters, node records) lives
 // in one file-scope __device__ array of fixed size.  The caller passes only its own
 // inputs and outputs; the call allocates nothing and needs no kwg_ctx.
 //
 // Rules of use:
 //   * Every GPU that loads this library holds the array (kStaticScratchBytes) until
 //     the process exits.
-//   * The first call on a device looks up the array's device address with that
-//     device current (cudaGetSymbolAddress) and caches it.  Make that first call
-//     before any stream capture.
+//   * Set-up: the first call on a device looks up the array's device address with
+//     that device current (cudaGetSymbolAddress) and caches it with the id of the
+//     device's CUDA context.  A later call whose current context has another id (the
+//     device was reset) or none yet (a host thread's first CUDA call) repeats the
+//     look-up.  Make the first call on each device, and from each host thread, before
+//     any stream capture.
 //   * All calls share the array and it keeps the last call's contents.  Each call
-//     clears what must start at zero (the tile queue and timeout flag) and rewrites
-//     everything else.  Calls that overlap on the GPU (two streams, or two host
-//     threads at once) race on the array: serialise them.
+//     clears what must start at zero (the class counters, the tile queue and the
+//     timeout flag) and rewrites everything else.  Calls that overlap on the GPU (two
+//     streams, or two host threads at once) race on the array: serialise them.
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -38,7 +42,11 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
 std::mutex g_mu;
-void* g_scratch_addr[kMaxDevices] = {};
+struct ScratchAddr {
+    void* ptr = nullptr;
+    unsigned long long ctx_id = 0;  // CUDA context the address belongs to
+};
+ScratchAddr g_scratch[kMaxDevices];
 
 size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 
@@ -47,7 +55,35 @@ void put(char* err, size_t errlen, const char* msg)
     if (err && errlen) std::snprintf(err, errlen, "%s", msg);
 }
 
-// The array's device address on the current device; looked up once per device.
+// cuCtxGetId of the driver API (CUDA 12.0+), reached through the runtime so the
+// library needs no link against libcuda; NULL asks for the current context.
+using CtxGetIdFn = int (*)(void* ctx, unsigned long long* id);
+
+CtxGetIdFn ctx_get_id()
+{
+    static CtxGetIdFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return (CtxGetIdFn)f;
+    }();
+    return fn;
+}
+
+// Id of the calling thread's current context; 0 if there is none (or no driver entry).
+unsigned long long current_ctx_id()
+{
+    unsigned long long id = 0;
+    const CtxGetIdFn fn = ctx_get_id();
+    if (!fn || fn(nullptr, &id) != 0) return 0;
+    return id;
+}
+
+// The array's device address on the current device.  Looked up (set-up) on the
+// first call for a device and again whenever the current context is not the one
+// the cached address belongs to.
 cudaError_t scratch_address(void** out)
 {
     int dev = 0;
@@ -55,32 +91,17 @@ cudaError_t scratch_address(void** out)
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_addr[dev]) {
+    ScratchAddr& c = g_scratch[dev];
+    const unsigned long long id = current_ctx_id();
+    if (!c.ptr || id == 0 || id != c.ctx_id) {
         void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_static_scratch);
+        e = cudaGetSymbolAddress(&p, g_static_scratch);  // makes the device's primary context current
         if (e != cudaSuccess) return e;
-        g_scratch_addr[dev] = p;
+        c.ptr = p;
+        c.ctx_id = current_ctx_id();
     }
-    *out = g_scratch_addr[dev];
+    *out = c.ptr;
     return cudaSuccess;
-}
-
-// AoS kw::Option -> SoA scratch arrays (every option is its own PDE).
-__global__ void unpack_static(const kwg_option* __restrict__ o, int n, double* t, double* z, double* r, double* q,
-                              double* s, double* k, int32_t* pde, int8_t* w, uint8_t* e)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const kwg_option a = o[i];
-    t[i] = a.t;
-    z[i] = a.z;
-    r[i] = a.r;
-    q[i] = a.q;
-    s[i] = a.s;
-    k[i] = a.k;
-    pde[i] = i;
-    w[i] = a.w;
-    e[i] = a.e;
 }
 
 }  // namespace
@@ -99,15 +120,27 @@ extern "C" int kwg_fd1d_price_device_static(const kwg_option* d_opts, size_t n, 
     if (!(p->scale > 0.) || !std::isfinite(p->scale))
         return put(err, errlen, "kwg: scale must be positive and finite"), KWG_ERR_INVALID;
     if (!(p->density > 0.)) return put(err, errlen, "kwg: density must be positive"), KWG_ERR_INVALID;
+    if (p->block_warps != 0 && p->block_warps != 1 && p->block_warps != 2 && p->block_warps != 4)
+        return put(err, errlen, "kwg: block_warps must be 0, 1, 2 or 4"), KWG_ERR_INVALID;
+    if (p->sm_blocks < 0 || p->sm_blocks > 64)
+        return put(err, errlen, "kwg: sm_blocks must be in [0, 64]"), KWG_ERR_INVALID;
+    if (p->strict)
+        return put(err, errlen,
+                   "kwg: strict mode applies to the blocking host calls only; this call is asynchronous, so read "
+                   "d_status"),
+               KWG_ERR_INVALID;
+    if (p->device_dedup)
+        return put(err, errlen, "kwg: the static-scratch call solves every option as its own PDE (no device_dedup)"),
+               KWG_ERR_INVALID;
     if (n == 0) return KWG_OK;
     if (!d_opts || !d_prices) return put(err, errlen, "kwg: null options or prices"), KWG_ERR_INVALID;
 
-    // scratch layout: SoA inputs | per-PDE status | 2 counters | node records
+    // scratch layout: SoA inputs | per-PDE status | class counters | solver counters | node records
     const size_t m = n, m_pad = (m + kwg::kTile - 1) / kwg::kTile * kwg::kTile;
     const bool huge = n > kStaticScratchBytes;  // cannot fit; also keeps the sums below from overflowing
     const size_t need = huge ? SIZE_MAX
-                             : 6 * align256(n * 8) + align256(n * 4) + 2 * align256(n) + align256(m_pad * 4) + 256 +
-                                   kwg::fd1d_fp64_work_bytes((int)m_pad, p->x_dim);
+                             : 6 * align256(n * 8) + align256(n * 4) + 2 * align256(n) + align256(m_pad * 4) +
+                                   2 * 256 + kwg::fd1d_fp64_work_bytes((int)m_pad, p->x_dim);
     if (huge || need > kStaticScratchBytes) {
         char msg[256];
         std::snprintf(msg, sizeof msg,
@@ -139,13 +172,18 @@ extern "C" int kwg_fd1d_price_device_static(const kwg_option* d_opts, size_t n, 
     int8_t* w = (int8_t*)take(n);
     uint8_t* e = (uint8_t*)take(n);
     int32_t* pde_status = (int32_t*)take(m_pad * 4);
+    int* classes = (int*)take(8 * sizeof(int));
     int* counters = (int*)take(4 * sizeof(int));
     double* rec = (double*)(s + o);
 
     cudaStream_t st = (cudaStream_t)stream;
     int dev = 0;
     cudaGetDevice(&dev);
-    unpack_static<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_opts, (int)n, t, z, r, q, sp, k, pde, w, e);
+    if (cudaError_t ce = kwg::unpack_by_class(d_opts, (int)n, classes, t, z, r, q, sp, k, pde, w, e, st);
+        ce != cudaSuccess) {
+        put(err, errlen, cudaGetErrorString(ce));
+        return KWG_ERR_CUDA;
+    }
 
     kwg::PdeBatch b;
     b.t = t;
@@ -169,7 +207,9 @@ extern "C" int kwg_fd1d_price_device_static(const kwg_option* d_opts, size_t n, 
     sh.scale = p->scale;
     sh.uniform = std::isinf(p->density);
     sh.density = sh.uniform ? 1. : p->density;
-    const int blocks = kwg::fd1d_fp64_solve_blocks((int)(m_pad / kwg::kTile), dev);
+    sh.block_warps = p->block_warps ? p->block_warps : 1;
+    sh.sm_blocks = p->sm_blocks;
+    const int blocks = kwg::fd1d_fp64_solve_blocks((int)(m_pad / kwg::kTile), dev, sh.block_warps, sh.sm_blocks);
     kwg::fd1d_fp64_launch(b, a, sh, rec, pde_status, counters, d_prices, d_status, blocks, st, nullptr);
     if (cudaError_t ce = cudaGetLastError(); ce != cudaSuccess) {
         put(err, errlen, cudaGetErrorString(ce));

@@ -98,6 +98,30 @@ def test_out_of_grid_status_and_strict(ctx):
     assert rc == kwg.KWG_ERR_OUT_OF_GRID and "not in grid range" in ctx.last_error()
 
 
+def test_device_call_refuses_strict_mode(ctx):
+    """The asynchronous device call cannot fail the call on a bad option without
+    waiting for the results, so it refuses strict = 1 before any launch; its caller
+    reads the per-option status instead."""
+    import torch
+
+    import kwg
+
+    g = golden("edge.npz")
+    o = g["bad_opts"]
+    d_o = torch.from_numpy(o.view(np.uint8).copy()).cuda()
+    d_p = torch.full((len(o),), float("nan"), dtype=torch.float64, device="cuda")
+    d_s = torch.full((len(o),), -1, dtype=torch.int32, device="cuda")
+    rc = ctx.fd1d_price_device(d_o.data_ptr(), len(o), kwg.params(strict=1), d_p.data_ptr(), d_s.data_ptr())
+    assert rc == kwg.KWG_ERR_INVALID and "strict" in ctx.last_error()
+    torch.cuda.synchronize()
+    assert torch.isnan(d_p).all()
+    rc = ctx.fd1d_price_device(d_o.data_ptr(), len(o), kwg.params(), d_p.data_ptr(), d_s.data_ptr())
+    assert rc == kwg.KWG_OK, ctx.last_error()
+    torch.cuda.synchronize()
+    st = d_s.cpu().numpy()
+    assert st[3] == kwg.STATUS_OUT_OF_GRID and (st[np.arange(8) != 3] == 0).all()
+
+
 @SOLVERS
 @pytest.mark.parametrize("theta", [0.6, 0.75, 1.0])
 def test_theta_other_than_half(ctx, theta, solver):
