@@ -14,12 +14,17 @@ Reported on one JSON line (rank 0):
              than L2, so no flush is needed between steps.
   e2e        the same metric through the reference-facing call (kwg_fd1d_price: host
              options in, host prices out; dedup, H2D and D2H inside the timing).
-  roofline   of the solve kernel, from its own CUDA events inside the timed region.
+  roofline   of the solve kernel, from its own CUDA events inside the timed region:
+             achieved = 32 B per node-step (the streaming scheme's algorithmic bytes)
+             over the launch time; the kernel's own count of requested bytes beside it.
   variants   FP64 and FP32 rates and their errors against the FP64 oracle.
   cpu_baseline  the oracle (C restatement of the reference, all host cores) on a
-             bounded sample of the same workload.
+             bounded sample of the same workload; its prices are the FP64 parity check
+             of the resident run.
 With --impl reference the reference's CPU implementation runs instead (oracle/_ref
-when it was built here from the reference sources, else the oracle port).
+when it was built here from the reference sources, else the oracle port, with the
+port/reference speed ratio measured by oracle/calibrate_port.py).  --gpus N without
+a launcher re-runs the script as N ranks through torch.distributed.run.
 """
 from __future__ import annotations
 
@@ -52,11 +57,23 @@ def node_steps(n, x_dim=None, t_dim=None):
     return n * (x_dim or X_DIM) * ((t_dim or T_DIM) - 1)
 
 
-# Algorithmic traffic of the FP64 streaming solve per node and step: V and the sweep
-# value read and written (32 B) plus, outside the uniform grid's frozen middle region,
-# three factor coefficients and the payoff (32 B; inside it only the payoff, 8 B).
-# The kernel counts these bytes itself (kwg_profile_read).
+# Traffic of the FP64 streaming solve per node and step: V and the sweep value read and
+# written (32 B, the algorithmic bytes of the scheme) plus what the kernel also reads:
+# outside the uniform grid's frozen middle region three factor coefficients (24 B),
+# and the payoff (8 B) where it is not +0 for the whole tile.  The kernel counts the
+# bytes it requests itself (kwg_profile_read).
 FP64_FLOPS_PER_NODE_STEP = 6  # 3 FMA per node-step at theta = 1/2
+ALGO_BYTES_PER_NODE_STEP = 32  # FP64 streaming scheme: V read + write, sweep value write + read
+
+
+def workload_config():
+    """The `config` both arms print (same keys and values, so the two lines compare)."""
+    return {"workload": WORKLOAD, "options_per_batch": N_OPTIONS, "x_dim": X_DIM, "t_dim": T_DIM, "theta": 0.5,
+            "scale": SCALE, "grid": "uniform", "precision": "fp64",
+            "l2": "working set 2.4 GB per step > 129 MB L2 (no flush needed)"}
+
+
+CALIBRATION_FILE = os.path.join(ROOT, "oracle", "port_calibration.json")
 
 
 def dist_env():
@@ -124,7 +141,9 @@ def peaks():
 
 
 def cpu_oracle_rate(opts_all, budget_s=12.0):
-    """The oracle (C restatement, all host cores) on a bounded sample of the workload."""
+    """The oracle (C restatement, all host cores) on a bounded sample of the workload:
+    the first n options of the batch, n grown until one call takes budget_s / 4.
+    Returns (options/s, threads, n, seconds, the n oracle prices)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import kwor
 
@@ -133,14 +152,55 @@ def cpu_oracle_rate(opts_all, budget_s=12.0):
     while True:
         sample = opts_all[:n]
         t0 = time.perf_counter()
-        rc, msg, _, _ = kwor.fd1d_price(sample, nthreads=threads, t_dim=T_DIM, x_dim=X_DIM, scale=SCALE,
-                                        density=DENSITY)
+        rc, msg, want, _ = kwor.fd1d_price(sample, nthreads=threads, t_dim=T_DIM, x_dim=X_DIM, scale=SCALE,
+                                           density=DENSITY)
         dt = time.perf_counter() - t0
         if rc != 0:
             raise RuntimeError(msg)
         if dt >= budget_s / 4 or n >= len(opts_all):
-            return n / dt, threads, n, dt
+            return n / dt, threads, n, dt, want
         n = min(len(opts_all), int(n * max(2.0, budget_s / 4 / max(dt, 1e-3))))
+
+
+def max_rel(got, want):
+    """Max relative error (prices of this workload are >= ~3e-4, so no floor is needed
+    beyond guarding an exact zero)."""
+    return float(np.max(np.abs(got - want) / np.maximum(np.abs(want), 1e-300)))
+
+
+def uneven_oracle_check(opts, x_dims, t_dims, prices, status, sample=4096):
+    """FP64 prices of the uneven batch against the oracle on an evenly spaced sample,
+    one oracle call per (x_dim, t_dim) group as the reference requires (one grid shape
+    per Fd1d_Pricer::init, src/Pricer/kwFd1d.cpp:15-16), the groups spread over the
+    host cores.  Out-of-grid status must agree; prices are compared where both are OK."""
+    import concurrent.futures as cf
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import kwor
+
+    idx = np.linspace(0, len(opts) - 1, min(sample, len(opts))).astype(np.int64)
+    groups = {}
+    for i in idx:
+        groups.setdefault((int(x_dims[i]), int(t_dims[i])), []).append(i)
+
+    def one(key):
+        ii = np.array(groups[key])
+        rc, msg, want, st = kwor.fd1d_price(opts[ii], nthreads=1, t_dim=key[1], x_dim=key[0], scale=SCALE,
+                                            density=DENSITY)
+        return ii, want, st
+
+    t0 = time.perf_counter()
+    worst, n_ok, status_mismatch = 0.0, 0, 0
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        for ii, want, st in ex.map(one, sorted(groups, key=lambda k: -k[0] * k[1])):
+            status_mismatch += int(((st != 0) != (status[ii] != 0)).sum())
+            ok = (st == 0) & (status[ii] == 0)
+            if ok.any():
+                worst = max(worst, max_rel(prices[ii][ok], want[ok]))
+                n_ok += int(ok.sum())
+    return {"max_rel_err_vs_oracle": worst, "oracle_sample": int(len(idx)), "oracle_sample_priced": n_ok,
+            "oracle_groups": len(groups), "status_mismatch": status_mismatch,
+            "oracle_s": time.perf_counter() - t0}
 
 
 def measured_traffic(ns):
@@ -175,18 +235,6 @@ def fp64_peak_tflops(dev):
     return best
 
 
-def fp64_error_sample(opts, gpu_prices, k=64):
-    """Max relative error of GPU FP64 prices against the oracle on an evenly spaced sample."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import kwor
-
-    idx = np.linspace(0, len(opts) - 1, k).astype(int)
-    rc, msg, want, _ = kwor.fd1d_price(opts[idx], t_dim=T_DIM, x_dim=X_DIM, scale=SCALE, density=DENSITY)
-    if rc != 0:
-        raise RuntimeError(msg)
-    return float(np.max(np.abs(gpu_prices[idx] - want) / np.abs(want))), int(k)
-
-
 def run_reference(args):
     """--impl reference: the reference's CPU implementation on the host cores."""
     ws, rank, _ = dist_env()
@@ -219,17 +267,25 @@ def run_reference(args):
     total = sum(one(args.warmup + i) for i in range(args.steps))
     value = per_step * args.steps / total
     cores = kwor.ref_lib().kwref_pool_size() if use_ref else threads
-    sample = (f"{per_step} options per step of the {N_OPTIONS}-option batch, 1024x1024, "
+    sample = (f"{per_step} options per step of the {N_OPTIONS}-option batch, {X_DIM}x{T_DIM}, "
               + ("reference src/ compiled from source, density 1e6 (its closest to uniform)" if use_ref
-                 else "oracle C restatement, uniform grid"))
+                 else "oracle C restatement (bit-exact port of the reference), uniform grid"))
+    baseline = {"value": value, "unit": "options/s", "cores": cores, "kind": kind, "sample": sample}
+    if not use_ref:
+        # the port's speed against the reference's own build, both timed on one host
+        # (oracle/calibrate_port.py): the reference is estimated at value / port_over_reference
+        try:
+            cal = json.load(open(CALIBRATION_FILE))
+            baseline["calibration"] = dict(cal, reference_estimate_options_per_sec=value / cal["port_over_reference"])
+        except (OSError, ValueError, KeyError):
+            baseline["calibration"] = None
     line = {
         "impl": "reference", "metric": "options_per_sec_fd64_1024x1024", "value": value, "unit": "options/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": value / REF_PUBLISHED_OPS, "dtype": "f64",
         "data": "synthetic (seeded splitmix64; American, S=100, K~U[80,120], vol~U[0.1,0.6], r,q~U[0,0.1], T~U[0.25,2])",
-        "config": {"workload": WORKLOAD, "options_per_batch": N_OPTIONS, "x_dim": X_DIM, "t_dim": T_DIM,
-                   "theta": 0.5, "scale": SCALE, "grid": "uniform", "precision": "fp64"},
-        "cpu_baseline": {"value": value, "unit": "options/s", "cores": cores, "kind": kind, "sample": sample},
+        "config": workload_config(),
+        "cpu_baseline": baseline,
         "e2e": {"value": value, "unit": "options/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -436,7 +492,7 @@ def run_ours(args):
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import kwor
 
-        idx = np.arange(0, N_OPTIONS, max(1, N_OPTIONS // 32))
+        idx = np.arange(0, N_OPTIONS, max(1, N_OPTIONS // 512))
         rcb, msgb, wantbs, _ = kwor.fd1d_price(opts[idx], bs=True, t_dim=T_DIM, x_dim=X_DIM, scale=SCALE,
                                                density=DENSITY)
         if rcb != 0:
@@ -472,6 +528,8 @@ def run_ours(args):
                             "failed_other": int(((st3 != 0) & (st3 != kwg.STATUS_OUT_OF_GRID)).sum())}
             if name == "fp64":
                 ref64 = pr3.copy()
+                if not args.no_cpu and rank == 0:
+                    uneven[name].update(uneven_oracle_check(o3, xd3, td3, pr3, st3))
             else:
                 ok = st3 == 0
                 e = np.abs(pr3[ok] - ref64[ok])
@@ -519,7 +577,7 @@ def run_ours(args):
             sys.path.insert(0, os.path.join(ROOT, "oracle"))
             import kwor
 
-            idx = np.linspace(0, len(o4) - 1, 16).astype(int)
+            idx = np.linspace(0, len(o4) - 1, 256).astype(int)
             rc4, msg4, want4, _ = kwor.fd1d_price(o4[idx], t_dim=2048, x_dim=2048, scale=SCALE, density=0.25)
             if rc4 != 0:
                 raise RuntimeError(msg4)
@@ -557,18 +615,32 @@ def run_ours(args):
     fp64_peak = fp64_peak_tflops(dev)
 
     # ---------------------------------------------------------------- roofline (solve kernel)
+    # achieved: the algorithmic bytes of the streaming two-sweep scheme, 32 B per
+    # node-step in FP64 (V read and written, the sweep value written and read back),
+    # over the solve kernel's CUDA-event time.  The kernel's own count of the bytes it
+    # requests (payoff and, outside the frozen middle region, coefficients on top) is
+    # reported beside it as achieved_requested.
     hbm, peak_src = peaks()
     per_launch_s = solve_ms / 1e3 / max(solve_n, 1)
     ns = node_steps(N_OPTIONS)
-    bytes_per_launch = solve_bytes / max(solve_n, 1)
-    achieved = bytes_per_launch / per_launch_s / 1e9
+    algo_bytes = ALGO_BYTES_PER_NODE_STEP * ns
+    achieved = algo_bytes / per_launch_s / 1e9
+    req_bytes = solve_bytes / max(solve_n, 1)
+    achieved_req = req_bytes / per_launch_s / 1e9
     fp64_tflops = FP64_FLOPS_PER_NODE_STEP * ns / per_launch_s / 1e12
     traffic = measured_traffic(ns)
 
-    err, nerr = fp64_error_sample(opts, gpu_prices)
-    if err > 1e-10:
-        raise RuntimeError(f"FP64 parity broken: max rel err {err:.3e} > 1e-10")
-    cpu_rate, cpu_threads, cpu_n, cpu_s = cpu_oracle_rate(opts) if not args.no_cpu else (None, 0, 0, 0.0)
+    # ---------------------------------------------------------------- CPU baseline and FP64 parity
+    # the oracle prices of the CPU-baseline sample are the parity check of the whole
+    # resident run (the first n options of the batch)
+    if not args.no_cpu:
+        cpu_rate, cpu_threads, cpu_n, cpu_s, cpu_want = cpu_oracle_rate(opts)
+        err, nerr = max_rel(gpu_prices[:cpu_n], cpu_want), cpu_n
+    else:
+        cpu_rate, cpu_threads, cpu_n, cpu_s = None, 0, 0, 0.0
+        err, nerr = None, 0
+    if err is not None and err > 1e-10:
+        raise RuntimeError(f"FP64 parity broken: max rel err {err:.3e} > 1e-10 on {nerr} options")
 
     line = {
         "metric": "options_per_sec_fd64_1024x1024",
@@ -583,17 +655,22 @@ def run_ours(args):
         "vs_baseline": value / REF_PUBLISHED_OPS,
         "dtype": "f64",
         "data": "synthetic (seeded splitmix64; American, S=100, K~U[80,120], vol~U[0.1,0.6], r,q~U[0,0.1], T~U[0.25,2])",
-        "config": {"workload": WORKLOAD, "options_per_batch": N_OPTIONS, "x_dim": X_DIM, "t_dim": T_DIM,
-                   "theta": 0.5, "scale": SCALE, "grid": "uniform", "precision": "fp64",
-                   "solver": tune64["solver"], "block_warps": tune64["block_warps"],
-                   "l2": "working set 2.7 GB per step > 129 MB L2 (no flush needed)"},
+        "config": workload_config(),
+        "launch": {"solver": tune64["solver"], "block_warps": tune64["block_warps"],
+                   "sm_blocks": tune64["sm_blocks"], "chosen_by": "kwg_autotune_ex on this shape"},
         "e2e": {"value": e2e_value, "unit": "options/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clk,
         "roofline": {"bound": "hbm", "kernel": "fd1d_solve_fp64", "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_src, "traffic": traffic,
-                     "algorithmic_bytes_per_launch": bytes_per_launch,
-                     "algorithmic_bytes_per_node_step": bytes_per_launch / ns,
+                     "algorithmic_bytes_per_launch": algo_bytes,
+                     "algorithmic_bytes_per_node_step": ALGO_BYTES_PER_NODE_STEP,
+                     "basis": "32 B per node-step (V read + write, sweep value write + read), FP64 streaming scheme",
+                     "achieved_requested": achieved_req, "frac_requested": achieved_req / hbm,
+                     "requested_bytes_per_node_step": req_bytes / ns,
+                     "requested_basis": "bytes the kernel itself requests (state 32 B + payoff 8 B where nonzero "
+                                        "+ coefficients 24 B outside the frozen middle region), counted in the kernel",
+                     "traffic_per_node_step": traffic / ns if traffic else None,
                      "node_steps_per_launch": ns, "launch_ms": per_launch_s * 1e3,
                      "fp64_tflops": fp64_tflops, "fp64_peak_tflops": fp64_peak,
                      "fp64_frac": fp64_tflops / fp64_peak if fp64_peak else None,
@@ -602,7 +679,8 @@ def run_ours(args):
                           "sample": f"{cpu_n} options of the batch at 1024x1024 ({cpu_s:.1f} s), oracle C "
                                     f"restatement, {cpu_threads} threads"} if cpu_rate else None),
         "variants": {"fd64": {"options_per_sec": value, "max_rel_err_vs_oracle": err,
-                              "oracle_sample": nerr},
+                              "oracle_sample": nerr,
+                              "oracle_sample_is": "the CPU-baseline sample: the first n options of the batch"},
                      "fd32": {"options_per_sec": value32, "ms_per_step": ms32 / args.steps,
                               "solve_ms": solve32_ms / max(solve32_n, 1),
                               "speedup_vs_fd64": value32 / value,
@@ -619,6 +697,19 @@ def run_ours(args):
                      "surrogate_1m": surrogate},
     }
     print(json.dumps(line), flush=True)
+
+
+def relaunch(n: int) -> int:
+    """--gpus N without a launcher: run this script as N ranks, one process per GPU,
+    through torch.distributed.run on this node (rendezvous on 127.0.0.1)."""
+    import socket
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr=127.0.0.1", f"--master-port={port}", os.path.abspath(__file__), *sys.argv[1:]]
+    return subprocess.call(cmd)
 
 
 def main():
@@ -640,6 +731,12 @@ def main():
     args = ap.parse_args()
     globals()["N_OPTIONS"] = args.options
     globals()["T_DIM"] = args.t_dim
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(relaunch(args.gpus))
+    ws = dist_env()[0]
+    if ws != args.gpus:
+        print(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={ws}; reporting the {ws} ranks that run",
+              file=sys.stderr)
     if args.impl == "reference":
         run_reference(args)
     else:
