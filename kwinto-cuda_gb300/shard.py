@@ -8,7 +8,8 @@ contiguous chunks, each priced by its own rank.  Two uses:
   * strong scaling: one portfolio partitioned after dedup into contiguous chunks
     balanced by x_dim * (t_dim - 1) node-steps (partition_by_work).
 The only cross-rank traffic is the timing reduction (max over ranks) and, for
-strong scaling, gathering 8-byte prices back to the caller.
+strong scaling, gathering 8-byte prices back to the caller (strong_shard,
+gather_prices).
 """
 from __future__ import annotations
 
@@ -45,6 +46,51 @@ def partition_by_work(x_dims, t_dims, world: int) -> list[tuple[int, int]]:
     bounds.append(len(x))
     bounds = [min(b, len(x)) for b in bounds]
     return [(bounds[r], bounds[r + 1]) for r in range(world)]
+
+
+def strong_shard(opts, rank: int, world: int, x_dim: int = 0, t_dim: int = 0, x_dims=None, t_dims=None):
+    """Indices of the options `rank` prices when one portfolio is split over `world`
+    ranks (strong scaling).  Every rank runs the same host dedup (kwg_fd1d_dedup, the
+    reference's key, src/Pricer/kwFd1d.cpp:28-65, plus the grid shape for uneven
+    batches), so all agree on the PDE list without exchanging it; the PDEs are cut
+    into contiguous chunks balanced by node-steps (partition_by_work) and a rank
+    takes every option whose PDE lies in its chunk, so no PDE is solved twice.  The
+    grid is x_dim x t_dim for every option, or x_dims[i] x t_dims[i] per option."""
+    import kwg
+
+    a2p, p2a = kwg.dedup(opts, x_dims, t_dims)
+    if len(p2a) == 0:
+        return np.zeros(0, np.int64)
+    if x_dims is not None and t_dims is not None:
+        xs, ts = np.asarray(x_dims)[p2a], np.asarray(t_dims)[p2a]
+    else:
+        xs, ts = np.full(len(p2a), x_dim), np.full(len(p2a), t_dim)
+    begin, end = partition_by_work(xs, ts, world)[rank]
+    return np.nonzero((a2p >= begin) & (a2p < end))[0]
+
+
+def gather_prices(n: int, idx, prices, status=None):
+    """All ranks' (indices, prices[, status]) assembled into arrays of the whole
+    portfolio on every rank: the only data that crosses ranks, 8 bytes (+4) per
+    option, after the solve.  Without a process group the rank's own arrays are
+    scattered into place."""
+    import torch.distributed as dist
+
+    mine = (np.asarray(idx, np.int64).tobytes(), np.asarray(prices, np.float64).tobytes(),
+            None if status is None else np.asarray(status, np.int32).tobytes())
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        parts = [None] * dist.get_world_size()
+        dist.all_gather_object(parts, mine)
+    else:
+        parts = [mine]
+    out = np.full(n, np.nan)
+    st = np.zeros(n, np.int32) if status is not None else None
+    for ib, pb, sb in parts:
+        ii = np.frombuffer(ib, np.int64)
+        out[ii] = np.frombuffer(pb, np.float64)
+        if st is not None and sb is not None:
+            st[ii] = np.frombuffer(sb, np.int32)
+    return out if st is None else (out, st)
 
 
 def max_over_ranks(value: float) -> float:
