@@ -62,15 +62,18 @@ __device__ __forceinline__ FF split(double v)
     return r;
 }
 
-// (h, l) + d with an error-free sum, renormalised.
-__device__ __forceinline__ void ff_add(float& h, float& l, float d)
+// (h, l) += d: h takes the rounded sum and l collects its rounding error, computed
+// by Fast2Sum (exact when |h| >= |d| or h == 0 -- the increment of a step is small
+// next to the value it updates; where it is not, V is near 0 and the loss is an ulp
+// of that tiny sum).  The pair is not renormalised: each step adds at most half an
+// ulp of h to l, so over a few thousand steps |l| stays within ~2^11 ulp(h), far
+// below h, and the differences of neighbouring h that the residual takes stay exact.
+__device__ __forceinline__ void ff_acc(float& h, float& l, float d)
 {
     const float s = h + d;
-    const float bb = s - h;
-    const float e = (h - (s - bb)) + (d - bb);
-    const float t = l + e;
-    h = s + t;
-    l = t - (h - s);
+    const float e = d - (s - h);
+    h = s;
+    l += e;
 }
 
 }  // namespace
@@ -479,7 +482,7 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
             // V += d (float-float), then the early-exercise floor on nodes < N-1
 #pragma unroll
             for (int i = 0; i < M; ++i) {
-                ff_add(H[i], Lo[i], y[i]);
+                ff_acc(H[i], Lo[i], y[i]);
                 if (amer && j0 + i < N - 1) {
                     const float ph = T(i, T_PH), pl = T(i, T_PL);
                     if ((H[i] - ph) + (Lo[i] - pl) < 0.f) {
