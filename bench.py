@@ -306,12 +306,21 @@ def surrogate_variant(args, ctx, rank, ws, fd32_rate, barrier, max_over_ranks):
     import kwg
     import portfolio
 
-    if not os.path.exists(SURROGATE_WEIGHTS):
-        return {"unavailable": "surrogate_weights.npz not trained (kwinto-cuda_gb300/train_surrogate.py)"}
     n = args.surrogate_options
-    net = kwg.Surrogate(torch.cuda.current_device())
-    net.load(SURROGATE_WEIGHTS)
-    meta = json.loads(str(np.load(SURROGATE_WEIGHTS)["meta"])) if "meta" in np.load(SURROGATE_WEIGHTS) else {}
+    if args.surrogate_train > 0:
+        # the network this run prices with is trained here, end to end: FD64 labels on
+        # the GPU, the library's tcgen05 training kernels, a held-out check
+        import train_surrogate
+
+        net, meta = train_surrogate.train(ctx, n=args.surrogate_train, grid=X_DIM)
+        meta["source"] = "trained in this run (train_surrogate.train)"
+    else:
+        if not os.path.exists(SURROGATE_WEIGHTS):
+            return {"unavailable": "surrogate_weights.npz not trained (kwinto-cuda_gb300/train_surrogate.py)"}
+        net = kwg.Surrogate(torch.cuda.current_device())
+        net.load(SURROGATE_WEIGHTS)
+        meta = json.loads(str(np.load(SURROGATE_WEIGHTS)["meta"])) if "meta" in np.load(SURROGATE_WEIGHTS) else {}
+        meta["source"] = "committed surrogate_weights.npz (metadata of the run that trained it)"
     opts = portfolio.american_portfolio(n, seed=5005, start=rank * n)
     fd = kwg.params(t_dim=T_DIM, x_dim=X_DIM, scale=SCALE, density=DENSITY, precision=kwg.FP32)
     # the FD32 launch shape for the audit's batch size (~1 % of the options), as a
@@ -382,21 +391,30 @@ def run_ours(args):
     # (a NULL stream handle would mean the context's own stream to the C ABI)
     stream = torch.cuda.Stream(dev)
 
-    # each rank prices its own batch (weak scaling), drawn from its own window of the stream
-    opts = shard.portfolio_shard(N_OPTIONS, rank, seed=42)
+    if args.scaling == "strong":
+        # one batch for the whole job: every rank deduplicates it alike and prices the
+        # options of its share of the PDEs (split by work); prices are gathered after
+        full = portfolio.american_portfolio(N_OPTIONS, seed=42)
+        own = shard.strong_shard(full, rank, ws, x_dim=X_DIM, t_dim=T_DIM)
+        opts = full[own]
+        n_loc, n_job = len(opts), N_OPTIONS
+    else:
+        # each rank prices its own batch (weak scaling), drawn from its own window of the stream
+        opts = shard.portfolio_shard(N_OPTIONS, rank, seed=42)
+        n_loc, n_job = N_OPTIONS, ws * N_OPTIONS
     prm = kwg.params(t_dim=T_DIM, x_dim=X_DIM, scale=SCALE, density=DENSITY, precision=kwg.FP64)
     d_opts = torch.from_numpy(opts.view(np.uint8).copy()).to(dev)
-    d_prices = torch.empty(N_OPTIONS, dtype=torch.float64, device=dev)
-    d_status = torch.empty(N_OPTIONS, dtype=torch.int32, device=dev)
+    d_prices = torch.empty(n_loc, dtype=torch.float64, device=dev)
+    d_status = torch.empty(n_loc, dtype=torch.int32, device=dev)
 
     # ---------------------------------------------------------------- autotuner: launch shapes
     # options per block and Thomas vs PCR (FP64), threads per option (FP32), on this shape
-    tune64 = ctx.autotune_ex(prm, N_OPTIONS).as_dict()
+    tune64 = ctx.autotune_ex(prm, n_loc).as_dict()
     tune32 = ctx.autotune_ex(kwg.params(t_dim=T_DIM, x_dim=X_DIM, scale=SCALE, density=DENSITY,
-                                        precision=kwg.FP32), N_OPTIONS).as_dict()
+                                        precision=kwg.FP32), n_loc).as_dict()
 
     def step(params=prm):
-        rc = ctx.fd1d_price_device(d_opts.data_ptr(), N_OPTIONS, params, d_prices.data_ptr(), d_status.data_ptr(),
+        rc = ctx.fd1d_price_device(d_opts.data_ptr(), n_loc, params, d_prices.data_ptr(), d_status.data_ptr(),
                                    stream.cuda_stream)
         if rc != 0:
             raise RuntimeError(ctx.last_error())
@@ -429,14 +447,19 @@ def run_ours(args):
     solve_ms, solve_n, solve_bytes = ctx.profile_read(with_bytes=True)
     ctx.set_profiling(False)
     ms = max_over_ranks(e0.elapsed_time(e1))
-    value = ws * N_OPTIONS * args.steps / (ms / 1e3)
+    value = n_job * args.steps / (ms / 1e3)
     status = d_status.cpu().numpy()
     gpu_prices = d_prices.cpu().numpy()
     if not (status == 0).all():
         raise RuntimeError(f"{int((status != 0).sum())} options failed")
+    if args.scaling == "strong":
+        # the 8-byte prices of every rank's share, assembled for the whole batch
+        whole = shard.gather_prices(N_OPTIONS, own, gpu_prices)
+        if np.isnan(whole).any():
+            raise RuntimeError("strong scaling: some options were priced by no rank")
 
     # ---------------------------------------------------------------- end to end (e2e)
-    prices_host = np.empty(N_OPTIONS)
+    prices_host = np.empty(n_loc)
     for _ in range(max(1, args.warmup)):
         rc, prices_host, _ = ctx.fd1d_price(opts, prm)
     barrier()
@@ -447,13 +470,13 @@ def run_ours(args):
             raise RuntimeError(ctx.last_error())
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     barrier()
-    e2e_value = ws * N_OPTIONS * args.steps / e2e_s
+    e2e_value = n_job * args.steps / e2e_s
     if not np.array_equal(prices_host, gpu_prices):
         raise RuntimeError("host and device entry points disagree")
     # bytes the host call moves per step (include/kwg.h packing): per PDE t,z,r,q (f64) + w,e;
     # per asset s,k (f64) + pde index (i32); back: price (f64) + status (i32) per asset.
-    h2d = N_OPTIONS * (4 * 8 + 2) + N_OPTIONS * (2 * 8 + 4)
-    d2h = N_OPTIONS * (8 + 4)
+    h2d = n_loc * (4 * 8 + 2) + n_loc * (2 * 8 + 4)
+    d2h = n_loc * (8 + 4)
 
     # ---------------------------------------------------------------- FP32 variant (resident)
     prm32 = kwg.params(t_dim=T_DIM, x_dim=X_DIM, scale=SCALE, density=DENSITY, precision=kwg.FP32)
@@ -470,7 +493,7 @@ def run_ours(args):
     solve32_ms, solve32_n = ctx.profile_read()
     ctx.set_profiling(False)
     ms32 = max_over_ranks(f0.elapsed_time(f1))
-    value32 = ws * N_OPTIONS * args.steps / (ms32 / 1e3)
+    value32 = n_job * args.steps / (ms32 / 1e3)
     p32 = d_prices.cpu().numpy()
     if not (d_status.cpu().numpy() == 0).all():
         raise RuntimeError("FP32: options failed")
@@ -486,13 +509,13 @@ def run_ours(args):
         if rc != 0:
             raise RuntimeError(ctx.last_error())
     dtbs = max_over_ranks(time.perf_counter() - t0) / args.steps
-    fd1d_bs = {"options_per_sec_e2e": ws * N_OPTIONS / dtbs, "ms_per_batch_e2e": dtbs * 1e3,
-               "pdes_solved": 2 * N_OPTIONS, "launches": ctx.launch_count()}
+    fd1d_bs = {"options_per_sec_e2e": n_job / dtbs, "ms_per_batch_e2e": dtbs * 1e3,
+               "pdes_solved": 2 * n_loc, "launches": ctx.launch_count()}
     if not args.no_cpu and rank == 0:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import kwor
 
-        idx = np.arange(0, N_OPTIONS, max(1, N_OPTIONS // 512))
+        idx = np.arange(0, n_loc, max(1, n_loc // 512))
         rcb, msgb, wantbs, _ = kwor.fd1d_price(opts[idx], bs=True, t_dim=T_DIM, x_dim=X_DIM, scale=SCALE,
                                                density=DENSITY)
         if rcb != 0:
@@ -622,7 +645,7 @@ def run_ours(args):
     # reported beside it as achieved_requested.
     hbm, peak_src = peaks()
     per_launch_s = solve_ms / 1e3 / max(solve_n, 1)
-    ns = node_steps(N_OPTIONS)
+    ns = node_steps(n_loc)
     algo_bytes = ALGO_BYTES_PER_NODE_STEP * ns
     achieved = algo_bytes / per_launch_s / 1e9
     req_bytes = solve_bytes / max(solve_n, 1)
@@ -651,7 +674,7 @@ def run_ours(args):
         "warmup": args.warmup,
         "ms_per_step": ms / args.steps,
         "higher_is_better": True,
-        "scaling": "weak",
+        "scaling": args.scaling,
         "vs_baseline": value / REF_PUBLISHED_OPS,
         "dtype": "f64",
         "data": "synthetic (seeded splitmix64; American, S=100, K~U[80,120], vol~U[0.1,0.6], r,q~U[0,0.1], T~U[0.25,2])",
@@ -719,11 +742,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--ref-options", type=int, default=256, help="options per reference step")
+    ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
+                    help="weak: every rank prices its own batch (default); strong: the ranks split one batch")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch (131072 options) variant")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate (1M options) variant")
     ap.add_argument("--no-fine-study", action="store_true", help="skip the 65536-option 2048x2048 precision study")
     ap.add_argument("--surrogate-options", type=int, default=SURROGATE_OPTIONS)
+    ap.add_argument("--surrogate-train", type=int, default=2_000_000,
+                    help="options to label and train the surrogate on in this run (0: load the committed weights)")
     ap.add_argument("--options", type=int, default=N_OPTIONS,
                     help="options per batch (default 32768; smaller values are for profiling captures)")
     ap.add_argument("--t-dim", type=int, default=T_DIM,

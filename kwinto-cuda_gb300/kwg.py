@@ -202,6 +202,7 @@ class Context:
 
     def __init__(self, device: int = 0):
         self._L = lib()
+        self.device = device
         self.ptr = self._L.kwg_create(device)
         if not self.ptr:
             raise RuntimeError(f"kwg_create({device}) failed: no usable CUDA device")

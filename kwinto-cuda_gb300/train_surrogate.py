@@ -66,6 +66,30 @@ def evaluate(net: kwg.Surrogate, ctx, n: int, grid: int, seed: int = TEST_SEED) 
             "p999_abs": float(np.quantile(err, 0.999)), "mean_abs": float(err.mean())}
 
 
+def train(ctx, n: int = 2_000_000, grid: int = 1024, epochs: int = 150, batch: int = 4096, lr: float = 2e-3,
+          seed: int = 1, test: int = 65536):
+    """Labels n options with FD64 on the GPU, trains a fresh network on them and
+    measures its held-out error on `test` fresh options: (network, metadata with the
+    measured label and training times)."""
+    import torch
+
+    opts = portfolio.american_portfolio(n, seed=TRAIN_SEED)
+    d_o = torch.from_numpy(opts.view(np.uint8).copy()).cuda()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d_p = fd64_device(ctx, d_o, n, grid)
+    t_label = time.perf_counter() - t0
+    net = kwg.Surrogate(ctx.device, seed=seed)
+    t0 = time.perf_counter()
+    loss = net.train(d_o.data_ptr(), d_p.data_ptr(), n, epochs, batch, lr, seed)
+    t_train = time.perf_counter() - t0
+    report = evaluate(net, ctx, test, grid)
+    meta = {"n_train": n, "grid": grid, "epochs": epochs, "batch": batch, "lr": lr, "seed": seed,
+            "label_s": t_label, "train_s": t_train, "final_loss": loss, "heldout": report}
+    del d_o, d_p
+    return net, meta
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--n", type=int, default=2_000_000, help="training options")
@@ -79,21 +103,8 @@ def main(argv=None):
                                                   "surrogate_weights.npz"))
     a = ap.parse_args(argv)
 
-    import torch
-
     ctx = kwg.Context(0)
-    opts = portfolio.american_portfolio(a.n, seed=TRAIN_SEED)
-    d_o = torch.from_numpy(opts.view(np.uint8).copy()).cuda()
-    t0 = time.perf_counter()
-    d_p = fd64_device(ctx, d_o, a.n, a.grid)
-    t_label = time.perf_counter() - t0
-    net = kwg.Surrogate(0, seed=a.seed)
-    t0 = time.perf_counter()
-    loss = net.train(d_o.data_ptr(), d_p.data_ptr(), a.n, a.epochs, a.batch, a.lr, a.seed)
-    t_train = time.perf_counter() - t0
-    report = evaluate(net, ctx, a.test, a.grid)
-    meta = {"n_train": a.n, "grid": a.grid, "epochs": a.epochs, "batch": a.batch, "lr": a.lr, "seed": a.seed,
-            "label_s": t_label, "train_s": t_train, "final_loss": loss, "heldout": report}
+    net, meta = train(ctx, a.n, a.grid, a.epochs, a.batch, a.lr, a.seed, a.test)
     p, lo, hi, ys = net.get_params()
     np.savez(a.out, params=p, box_lo=lo, box_hi=hi, y_scale=np.float32(ys), meta=json.dumps(meta))
     print(json.dumps(meta))
