@@ -36,18 +36,20 @@ namespace kwg {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-// table fields per node, layout [node-in-lane][field][lane] (conflict-free).  On a
-// uniform grid without padded nodes the interior rows of B are the same at every
-// node, so
+// Tables per node, grouped by the step that reads them so that each group is one
+// vector load: the payoff pair (PH, PL); the forward-elimination pair (L, ID); U of
+// the back substitution; the two spike values (SL, SR); and, on non-uniform grids,
+// the residual coefficients (C1, C2, C3, C4).  Per-lane groups are laid out
+// [node-in-lane][lane] (consecutive lanes, conflict-free).  On a uniform grid
+// without padded nodes the interior rows of B are the same at every node, so
 //   * the residual coefficients c1..c4 live in registers;
 //   * every lane but the last has the same interior block B_I, hence the same LU
-//     factors and spikes: those 5 fields are kept once for the group plus once for
-//     the last lane (whose block holds the boundary row), [node][field][2], read as
-//     broadcasts; only the payoff pair stays per lane.
-enum { T_L = 0, T_ID, T_U, T_SL, T_SR, T_PH, T_PL, T_C1, T_C2, T_C3, T_C4 };
+//     factors and spikes: (L, ID), U and (SL, SR) are kept once for the group plus
+//     once for the last lane (whose block holds the boundary row), [node][2], read
+//     as broadcasts; only the payoff pair stays per lane.
 template <bool kUni>
-__host__ __device__ constexpr int f32_fields() { return kUni ? 2 : 11; }  // per-lane fields
-constexpr int kSharedFields = 5;                                          // T_L .. T_SR
+__host__ __device__ constexpr int f32_fields() { return kUni ? 2 : 11; }  // per-lane floats per node
+constexpr int kSharedFields = 5;                                          // L, ID, U, SL, SR
 
 struct FF {
     float hi, lo;
@@ -76,7 +78,32 @@ __device__ __forceinline__ void ff_acc(float& h, float& l, float d)
     l += e;
 }
 
+// Packed FP32 pairs (two FP32 operations per instruction on sm_100 and later).
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
+
+// ff_acc on two independent float-float values at once.
+__device__ __forceinline__ void ff_acc2(float2& h, float2& l, float2 d)
+{
+    const float2 s = __fadd2_rn(h, d);
+    const float2 e = sub2(d, sub2(s, h));
+    h = s;
+    l = __fadd2_rn(l, e);
+}
+
 }  // namespace
+
+// Uniform grids, one warp per PDE, at least 4 nodes per lane: the step runs on packed
+// FP32 pairs.  A lane's nodes are paired around its pivot row P = M/2 -- slot k holds
+// nodes (P-k, P+k) for k = 1 .. P-1, slot 0 nodes (0, P) -- so that the two chains of
+// the twisted interior solve, which walk P-k and P+k in step, are the two halves of
+// one packed operation, and so are the per-node residual, spike and update.  The
+// tables are repacked by slot after the setup: the payoff as (hi(P-k), hi(P+k),
+// lo(P-k), lo(P+k)) per lane, the shared factors as three float4 per slot.
+template <int M, bool kUni, int W>
+__host__ __device__ constexpr bool f32_paired() { return kUni && W == 1 && M >= 4; }
+template <int M, bool kUni, int W>
+__host__ __device__ constexpr int f32_pair_floats() { return f32_paired<M, kUni, W>() ? 2 * M * 32 + 12 * M : 0; }
 
 // Shared-memory bytes of the lane-exchange area of a W-warp PDE group (W > 1).
 template <int W>
@@ -95,25 +122,57 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
     constexpr int kF = f32_fields<kUni>();
     constexpr int NL = 32 * W;
     constexpr int kLevels = W == 1 ? 5 : W == 2 ? 6 : W == 4 ? 7 : 8;  // log2 of the lanes
+    constexpr int kPivot = M / 2;  // pivot row of the twisted interior factorisation
+    static_assert(M % 2 == 0, "an even number of nodes per lane: as many rows above the pivot as below");
     static_assert(W == 1 || W == 2 || W == 4 || W == 8, "1, 2, 4 or 8 warps per PDE");
-    // [M][kF][NL] per-lane fields, then (uniform) [M][5][2] shared factors, then the
-    // exchange area (W > 1)
+    // Tables: non-uniform grids C [M][NL] float4, then PAY, LID, SPK [M][NL] float2,
+    // then U [M][NL]; uniform grids PAY [M][NL] float2, then the shared factors LID,
+    // SPK [M][2] float2 and U [M][2]; then the exchange area (W > 1).
     extern __shared__ float tab[];
     const int k = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int K = threadIdx.x;  // lane of the PDE group
     constexpr int kTabFloats = M * kF * NL + (kUni ? M * kSharedFields * 2 : 0);
-    // this lane's copy of the shared factors: +1 for the last lane only, computed
-    // arithmetically ((K + 1) / NL with NL a power of two) so that the loads stay
-    // single loads from one base address
-    float* const shr = tab + M * kF * NL + (K + 1) / NL;
+    // per-lane groups at [i * NL + K]; the uniform grid's shared groups at [i * 2 + c]
+    // with c = 1 for the last lane only, computed arithmetically ((K + 1) / NL with NL
+    // a power of two) so that the loads stay single loads from one base address
+    constexpr int kLane0 = kUni ? 0 : 4 * M * NL;  // floats before PAY
+    float2* const pay = reinterpret_cast<float2*>(tab + kLane0) + K;
+    float4* const cof = reinterpret_cast<float4*>(tab) + K;
+    constexpr int kStride = kUni ? 2 : NL;  // elements per node of the factor groups
+    const int own = kUni ? (K + 1) / NL : K;
+    float2* const lid = reinterpret_cast<float2*>(tab + kLane0 + 2 * M * NL) + own;
+    float2* const spk = lid + M * kStride;
+    float* const ufac = reinterpret_cast<float*>(tab + kLane0 + 2 * M * NL + 4 * M * kStride) + own;
     // uniform grid: lane 0 writes the group's factors, the last lane its own
     const bool writer = !kUni || K == 0 || K == NL - 1;
-    auto T = [&](int i, int f) -> float& {
-        if constexpr (kUni) {
-            if (f >= T_PH) return tab[(i * kF + (f - T_PH)) * NL + K];
-            return shr[(i * kSharedFields + f) * 2];
-        } else {
-            return tab[(i * kF + f) * NL + K];
+    auto PAY = [&](int i) -> float2& { return pay[i * NL]; };
+    auto LID = [&](int i) -> float2& { return lid[i * kStride]; };
+    auto SPK = [&](int i) -> float2& { return spk[i * kStride]; };
+    auto U = [&](int i) -> float& { return ufac[i * kStride]; };
+    auto C = [&](int i) -> float4& { return cof[i * NL]; };
+    // B_I^-1 v in place on nodes 1 .. M-1 by a twisted factorisation: eliminate from
+    // both ends towards node kPivot (two independent chains), solve that row, then
+    // substitute back outward (two chains again).  Tables: rows above the pivot
+    // (L, ID) = (l_i, 1/d_i), U = bu_i/d_i of the top-down LU; rows below it
+    // (m_i, 1/e_i), bl_i/e_i of the bottom-up elimination; the pivot row (l_P, 1/gamma)
+    // and U = m_P.
+    auto interior_solve = [&](float (&v)[M]) {
+        float f = 0.f, g = 0.f;
+#pragma unroll
+        for (int jj = 0; jj < kPivot - 1; ++jj) {
+            const int it = 1 + jj, ib = M - 1 - jj;
+            f = fmaf(-LID(it).x, f, v[it]);
+            v[it] = f;
+            g = fmaf(-LID(ib).x, g, v[ib]);
+            v[ib] = g;
+        }
+        const float2 lp = LID(kPivot);
+        v[kPivot] = fmaf(-U(kPivot), g, fmaf(-lp.x, f, v[kPivot])) * lp.y;
+#pragma unroll
+        for (int jj = 0; jj < kPivot - 1; ++jj) {
+            const int it = kPivot - 1 - jj, ib = kPivot + 1 + jj;
+            v[it] = fmaf(-U(it), v[it + 1], v[it] * LID(it).y);
+            v[ib] = fmaf(-U(ib), v[ib - 1], v[ib] * LID(ib).y);
         }
     };
     const int j0 = K * M;
@@ -174,6 +233,8 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
         double bla = 0., ba = 1., bua = 0.;          // separator row (node kM)
         double L1 = 0., Llast = 0., R1 = 0., Rlast = 0.;
         double bl_first_f = 0., bu_last_f = 0.;   // first interior bl, last interior bu
+        // pivot row P of the twisted factorisation: its row and top multiplier
+        double bl_piv = 0., b_piv = 1., bu_piv = 0., l_piv = 0., bu_above = 0.;
         {
             double xm = (j0 > 0 && j0 - 1 < N) ? g.x(j0 - 1) : 0.;
             double x0 = (j0 < N) ? g.x(j0) : 0.;
@@ -206,14 +267,8 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
                     // the payoff is exactly 0 on the out-of-the-money side: skip exp there
                     if ((w < 0) ? (x0 < 0.) : (x0 > 0.)) p = split(payoff(w, x0));
                 }
-                if (!kUni) {
-                    T(i, T_C1) = c1;
-                    T(i, T_C2) = c2;
-                    T(i, T_C3) = c3;
-                    T(i, T_C4) = c4;
-                }
-                T(i, T_PH) = p.hi;
-                T(i, T_PL) = p.lo;
+                if (!kUni) C(i) = make_float4(c1, c2, c3, c4);
+                PAY(i) = make_float2(p.hi, p.lo);
                 if (i == 0) {
                     bla = bl;
                     ba = bb;
@@ -225,10 +280,16 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
                     if (!(d != 0.) || !isfinite(d)) st = st == KWG_STATUS_OK ? KWG_STATUS_SOLVER : st;
                     const double idd = 1. / d;
                     const double u = bu * idd;
-                    if (writer) {
-                        T(i, T_L) = (float)l;
-                        T(i, T_ID) = (float)idd;
-                        T(i, T_U) = (float)u;
+                    if (writer && i < kPivot) {
+                        LID(i) = make_float2((float)l, (float)idd);
+                        U(i) = (float)u;
+                    }
+                    if (i == kPivot) {
+                        bl_piv = bl;
+                        b_piv = bb;
+                        bu_piv = bu;
+                        l_piv = l;
+                        bu_above = bu_prev;
                     }
                     // spike ends: L = B_I^-1 (bl_1 e_1), R = B_I^-1 (bu_{M-1} e_{M-1}).
                     // L_1 = bl_1 (B_I^-1)_11 = bl_1 sum_k prod_{i<k}(-u_i) / d_k prod_{2<=i<=k}(-l_i)
@@ -259,28 +320,57 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
             R1 = Rlast * pr;
             bl_first_f = bl_first;
         }
-        // full spike arrays for the per-step correction, in FP32 from the stored LU
+        // Bottom part of the twisted factorisation of B_I (rows M-1 .. kPivot+1,
+        // eliminating upward from the lane's last node) and the pivot row kPivot:
+        //   e_i = b_i - m_i bl_{i+1},  m_i = bu_i / e_{i+1}  (m_{M-1} = 0),
+        //   gamma = b_P - l_P bu_{P-1} - m_P bl_{P+1}.
         if (writer) {
-            float f = (float)bl_first_f;
+            double e_next = 1., bl_next = 0.;
+            const int jt = j0 + M - 1;
+            double xp = (jt + 1 < N) ? g.x(jt + 1) : 0., x0 = (jt < N) ? g.x(jt) : 0.;
 #pragma unroll 1
-            for (int i = 1; i < M; ++i) {
-                if (i > 1) f = -T(i, T_L) * f;
-                T(i, T_SL) = f * T(i, T_ID);
+            for (int i = M - 1; i > kPivot; --i) {
+                const int j = j0 + i;
+                const double xm = (j - 1 < N) ? g.x(j - 1) : 0.;
+                double bl = 0., bb = 1., bu = 0.;
+                if (j < N) {
+                    const Row rw = implicit_row(j, N, xm, x0, xp, sh.theta, dt, a.a0, a.ax, a.axx);
+                    bl = rw.bl;
+                    bb = rw.b;
+                    bu = rw.bu;
+                }
+                const double m = (i == M - 1) ? 0. : bu / e_next;
+                const double e = (i == M - 1) ? bb : bb - m * bl_next;
+                if (!(e != 0.) || !isfinite(e)) st = st == KWG_STATUS_OK ? KWG_STATUS_SOLVER : st;
+                const double ie = 1. / e;
+                LID(i) = make_float2((float)m, (float)ie);
+                U(i) = (float)(bl * ie);
+                e_next = e;
+                bl_next = bl;
+                xp = x0;
+                x0 = xm;
             }
-            float nxt = 0.f;
-#pragma unroll 1
-            for (int i = M - 1; i >= 1; --i) {
-                const float v = (i == M - 1) ? T(i, T_SL) : T(i, T_SL) - T(i, T_U) * nxt;
-                T(i, T_SL) = v;
-                nxt = v;
-            }
-            float rn = (float)bu_last_f * T(M - 1, T_ID);
-            T(M - 1, T_SR) = rn;
-#pragma unroll 1
-            for (int i = M - 2; i >= 1; --i) {
-                rn = -T(i, T_U) * rn;
-                T(i, T_SR) = rn;
-            }
+            const double m_piv = (kPivot == M - 1) ? 0. : bu_piv / e_next;
+            const double gam = b_piv - l_piv * bu_above - m_piv * bl_next;
+            if (!(gam != 0.) || !isfinite(gam)) st = st == KWG_STATUS_OK ? KWG_STATUS_SOLVER : st;
+            (void)bl_piv;
+            LID(kPivot) = make_float2((float)l_piv, (float)(1. / gam));
+            U(kPivot) = (float)m_piv;
+            // spikes L = B_I^-1 (bl_1 e_1) and R = B_I^-1 (bu_{M-1} e_{M-1}), by the
+            // same FP32 solve the steps use
+            float v[M];
+#pragma unroll
+            for (int i = 0; i < M; ++i) v[i] = 0.f;
+            v[1] = (float)bl_first_f;
+            interior_solve(v);
+#pragma unroll
+            for (int i = 1; i < M; ++i) SPK(i).x = v[i];
+#pragma unroll
+            for (int i = 0; i < M; ++i) v[i] = 0.f;
+            v[M - 1] = (float)bu_last_f;
+            interior_solve(v);
+#pragma unroll
+            for (int i = 1; i < M; ++i) SPK(i).y = v[i];
         }
         // separator system (FP64) and its cyclic-reduction multipliers (stored FP32)
         float ka[kLevels], kc[kLevels], ib;
@@ -364,81 +454,126 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
             else
                 __syncthreads();
         }
-        float H[M], Lo[M];  // V as float-float pairs, starting at the payoff
+        if constexpr (f32_paired<M, kUni, W>()) {
+            constexpr int P = M / 2;
+            // repack the tables by slot (node P-k and P+k; slot 0: node 0 and the pivot P)
+            float4* const ppay = reinterpret_cast<float4*>(tab + kTabFloats) + K;          // [P][NL]
+            float4* const pfac = reinterpret_cast<float4*>(tab + kTabFloats + 4 * P * NL) + 3 * own;  // [P][2][3]
 #pragma unroll
-        for (int i = 0; i < M; ++i) {
-            H[i] = T(i, T_PH);
-            Lo[i] = T(i, T_PL);
-        }
-
-        // ------------------------------------------------------------ time steps
-        for (int step = 1; run && step < TL; ++step) {
-            float Hm, Lm, Hp, Lp;
-            if constexpr (W == 1) {
-                Hm = __shfl_up_sync(kFull, H[M - 1], 1);
-                Lm = __shfl_up_sync(kFull, Lo[M - 1], 1);
-                Hp = __shfl_down_sync(kFull, H[0], 1);
-                Lp = __shfl_down_sync(kFull, Lo[0], 1);
-            } else {
-                x_last[K] = make_float2(H[M - 1], Lo[M - 1]);
-                x_first[K] = make_float2(H[0], Lo[0]);
-                __syncthreads();
-                const float2 pm = x_last[K > 0 ? K - 1 : 0], pp = x_first[K < NL - 1 ? K + 1 : 0];
-                Hm = pm.x;
-                Lm = pm.y;
-                Hp = pp.x;
-                Lp = pp.y;
+            for (int kk = 0; kk < P; ++kk) {
+                const float2 pa = PAY(kk == 0 ? 0 : P - kk), pb = PAY(P + kk);
+                ppay[kk * NL] = make_float4(pa.x, pb.x, pa.y, pb.y);
             }
-            if (K == 0) Hm = Lm = 0.f;
-            if (K == NL - 1) Hp = Lp = 0.f;
-            float y[M];
-            // residual r = dt A V from exact float-float differences
+            if (writer) {
 #pragma unroll
-            for (int i = 0; i < M; ++i) {
-                const float hl = (i == 0) ? Hm : H[i - 1], ll = (i == 0) ? Lm : Lo[i - 1];
-                const float hr = (i == M - 1) ? Hp : H[i + 1], lr = (i == M - 1) ? Lp : Lo[i + 1];
-                const float hdu = hr - H[i], hdd = H[i] - hl, ldu = lr - Lo[i], ldd = Lo[i] - ll;
-                const float Dup = hdu + ldu, Ddn = hdd + ldd, S = (hdu - hdd) + (ldu - ldd);
-                if (kUni) {
-                    float r = c4u * (H[i] + Lo[i]);
+                for (int kk = 0; kk < P; ++kk) {
+                    const int na = kk == 0 ? P : P - kk, nb = P + kk;  // slot 0: the pivot row twice
+                    const float2 la = LID(na), lb = LID(nb), sa = SPK(na), sb = SPK(nb);
+                    pfac[kk * 6 + 0] = make_float4(la.x, lb.x, la.y, lb.y);
+                    pfac[kk * 6 + 1] = make_float4(U(na), U(nb), sa.x, sb.x);
+                    pfac[kk * 6 + 2] = make_float4(sa.y, sb.y, 0.f, 0.f);
+                }
+            }
+            __syncwarp();
+            float2 H2[P], L2[P];  // V as float-float pairs by slot, starting at the payoff
+#pragma unroll
+            for (int kk = 0; kk < P; ++kk) {
+                const float4 p = ppay[kk * NL];
+                H2[kk] = make_float2(p.x, p.y);
+                L2[kk] = make_float2(p.z, p.w);
+            }
+            // residual coefficients by component: .x of slot k is node P-k, whose upward
+            // difference is D_k.x; .y is node P+k, whose upward difference is -D_(k+1).y
+            const float2 c4v = make_float2(c4u, c4u), c1v = make_float2(c1u, c1u);
+            const float2 c23 = make_float2(c2u, -c3u), c32 = make_float2(c3u, -c2u);
+            for (int step = 1; run && step < TL; ++step) {
+                float Hm = __shfl_up_sync(kFull, H2[P - 1].y, 1);
+                float Lm = __shfl_up_sync(kFull, L2[P - 1].y, 1);
+                float Hp = __shfl_down_sync(kFull, H2[0].x, 1);
+                float Lp = __shfl_down_sync(kFull, L2[0].x, 1);
+                if (K == 0) Hm = Lm = 0.f;
+                if (K == NL - 1) Hp = Lp = 0.f;
+                // differences of consecutive slots, D_k = V_(k-1) - V_k (k = 1 .. P), with the
+                // pivot in both components before slot 1 and (node 0, node M) after slot P-1:
+                // .x = V(P-k+1) - V(P-k), .y = V(P+k-1) - V(P+k), hi and lo parts exactly
+                auto diff = [&](int kk, float2& dh, float2& dl) {
+                    const float2 hu = kk == 1 ? make_float2(H2[0].y, H2[0].y) : H2[kk - 1];
+                    const float2 lu = kk == 1 ? make_float2(L2[0].y, L2[0].y) : L2[kk - 1];
+                    const float2 hd = kk == P ? make_float2(H2[0].x, Hp) : H2[kk];
+                    const float2 ld = kk == P ? make_float2(L2[0].x, Lp) : L2[kk];
+                    dh = sub2(hu, hd);
+                    dl = sub2(lu, ld);
+                };
+                float2 y2[P];
+                float2 dh1, dl1, dhP, dlP;
+                diff(1, dh1, dl1);
+                float2 dh = dh1, dl = dl1, d = __fadd2_rn(dh1, dl1);
+#pragma unroll
+                for (int kk = 1; kk < P; ++kk) {
+                    float2 dhn, dln;
+                    diff(kk + 1, dhn, dln);
+                    const float2 dn = __fadd2_rn(dhn, dln);
+                    const float2 S = __fadd2_rn(sub2(dh, dhn), sub2(dl, dln));
+                    float2 r = __fmul2_rn(c4v, __fadd2_rn(H2[kk], L2[kk]));
+                    r = __ffma2_rn(c1v, S, r);
+                    r = __ffma2_rn(c23, d, r);
+                    y2[kk] = __ffma2_rn(c32, dn, r);
+                    dh = dhn;
+                    dl = dln;
+                    d = dn;
+                }
+                dhP = dh;
+                dlP = dl;
+                // the pivot P and the separator 0, node by node
+                float yP, y0;
+                {
+                    const float hdu = -dh1.y, hdd = dh1.x, ldu = -dl1.y, ldd = dl1.x;
+                    const float Dup = hdu + ldu, Ddn = hdd + ldd, S = (hdu - hdd) + (ldu - ldd);
+                    float r = c4u * (H2[0].y + L2[0].y);
                     r = fmaf(c1u, S, r);
                     r = fmaf(c2u, Dup, r);
-                    y[i] = fmaf(c3u, Ddn, r);
-                } else {
-                    float r = T(i, T_C4) * (H[i] + Lo[i]);
-                    r = fmaf(T(i, T_C1), S, r);
-                    r = fmaf(T(i, T_C2), Dup, r);
-                    y[i] = fmaf(T(i, T_C3), Ddn, r);
+                    yP = fmaf(c3u, Ddn, r);
                 }
-            }
-            if (kUni) {  // the one-sided boundary rows (no second difference)
-                if (K == 0) y[0] = fmaf(c2b, (H[1] - H[0]) + (Lo[1] - Lo[0]), c4u * (H[0] + Lo[0]));
-                if (K == NL - 1)
-                    y[M - 1] = fmaf(c3b, (H[M - 1] - H[M - 2]) + (Lo[M - 1] - Lo[M - 2]), c4u * (H[M - 1] + Lo[M - 1]));
-            }
-            // interior: forward and backward Thomas
-            {
-                float f = 0.f;
-#pragma unroll
-                for (int i = 1; i < M; ++i) {
-                    f = fmaf(-T(i, T_L), f, y[i]);
-                    y[i] = f * T(i, T_ID);
+                {
+                    const float hdu = dhP.x, hdd = H2[0].x - Hm, ldu = dlP.x, ldd = L2[0].x - Lm;
+                    const float Dup = hdu + ldu, Ddn = hdd + ldd, S = (hdu - hdd) + (ldu - ldd);
+                    float r = c4u * (H2[0].x + L2[0].x);
+                    r = fmaf(c1u, S, r);
+                    r = fmaf(c2u, Dup, r);
+                    y0 = fmaf(c3u, Ddn, r);
+                    // the one-sided boundary rows (no second difference): node 0 of the first
+                    // lane, node M-1 (slot P-1 .y) of the last
+                    if (K == 0) y0 = fmaf(c2b, hdu + ldu, c4u * (H2[0].x + L2[0].x));
                 }
+                if (K == NL - 1) {
+                    const float2 dm = sub2(H2[P - 1], H2[P - 2 > 0 ? P - 2 : 0]);
+                    const float2 lm = sub2(L2[P - 1], L2[P - 2 > 0 ? P - 2 : 0]);
+                    // node M-1 minus node M-2 (for P = 2 node M-2 is the pivot, slot 0 .y)
+                    y2[P - 1].y = fmaf(c3b, dm.y + lm.y, c4u * (H2[P - 1].y + L2[P - 1].y));
+                }
+                // interior: twisted elimination, both chains in one packed operation ...
+                float2 F = make_float2(0.f, 0.f);
 #pragma unroll
-                for (int i = M - 2; i >= 1; --i) y[i] = fmaf(-T(i, T_U), y[i + 1], y[i]);
-            }
-            // separators: right-hand side, cyclic reduction, back to the interior
-            float ylp;
-            if constexpr (W == 1) {
-                ylp = __shfl_up_sync(kFull, y[M - 1], 1);
-            } else {
-                x_y[K] = y[M - 1];
-                __syncthreads();
-                ylp = x_y[K > 0 ? K - 1 : 0];
-            }
-            if (K == 0) ylp = 0.f;
-            float rho = y[0] - blaf * ylp - buaf * y[1];
-            if constexpr (W == 1) {
+                for (int kk = P - 1; kk >= 1; --kk) {
+                    const float4 f0 = pfac[kk * 6];
+                    F = __ffma2_rn(make_float2(-f0.x, -f0.y), F, y2[kk]);
+                    y2[kk] = F;
+                }
+                // ... the pivot row ...
+                const float4 fp0 = pfac[0], fp1 = pfac[1], fp2 = pfac[2];
+                yP = fmaf(-fp1.y, F.y, fmaf(-fp0.y, F.x, yP)) * fp0.w;
+                // ... and the back substitution outward
+                float2 X = make_float2(yP, yP);
+#pragma unroll
+                for (int kk = 1; kk < P; ++kk) {
+                    const float4 f0 = pfac[kk * 6], f1 = pfac[kk * 6 + 1];
+                    X = __ffma2_rn(make_float2(-f1.x, -f1.y), X, __fmul2_rn(y2[kk], make_float2(f0.z, f0.w)));
+                    y2[kk] = X;
+                }
+                // separators: right-hand side, cyclic reduction, back to the interior
+                float ylp = __shfl_up_sync(kFull, y2[P - 1].y, 1);  // lane K-1's node M-1
+                if (K == 0) ylp = 0.f;
+                float rho = y0 - blaf * ylp - buaf * y2[P - 1].x;  // node 1 is slot P-1 .x
 #pragma unroll
                 for (int lv = 0; lv < kLevels; ++lv) {
                     const int sg = 1 << lv;
@@ -446,57 +581,172 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
                     const float rp = __shfl_down_sync(kFull, rho, sg);
                     rho = rho - ka[lv] * rm - kc[lv] * rp;
                 }
-            } else {
-                float* cur = x_p0;
-                float* nxt = x_p1;
-                cur[K] = rho;
-                __syncthreads();
+                const float sv = rho * ib;
+                float s1 = __shfl_down_sync(kFull, sv, 1);
+                if (K == NL - 1) s1 = 0.f;
+                const float2 ms = make_float2(-sv, -sv), ms1 = make_float2(-s1, -s1);
 #pragma unroll
-                for (int lv = 0; lv < kLevels; ++lv) {
-                    const int sg = 1 << lv;
-                    const float rm = cur[K - sg >= 0 ? K - sg : K];
-                    const float rp = cur[K + sg < NL ? K + sg : K];
-                    rho = rho - ka[lv] * rm - kc[lv] * rp;  // ka, kc are 0 past the ends
-                    if (lv + 1 < kLevels) {
-                        nxt[K] = rho;
-                        __syncthreads();
-                        float* tmp = cur;
-                        cur = nxt;
-                        nxt = tmp;
+                for (int kk = 1; kk < P; ++kk) {
+                    const float4 f1 = pfac[kk * 6 + 1], f2 = pfac[kk * 6 + 2];
+                    y2[kk] = __ffma2_rn(ms1, make_float2(f2.x, f2.y), __ffma2_rn(ms, make_float2(f1.z, f1.w), y2[kk]));
+                }
+                y2[0] = make_float2(sv, fmaf(-s1, fp2.x, fmaf(-sv, fp1.z, yP)));
+                // V += d (float-float), then the early-exercise floor on nodes < N-1 (all but
+                // the last lane's node M-1, slot P-1 .y)
+#pragma unroll
+                for (int kk = 0; kk < P; ++kk) {
+                    ff_acc2(H2[kk], L2[kk], y2[kk]);
+                    if (amer) {
+                        const float4 p = ppay[kk * NL];
+                        const float2 e = __fadd2_rn(sub2(H2[kk], make_float2(p.x, p.y)), sub2(L2[kk], make_float2(p.z, p.w)));
+                        if (e.x < 0.f) {
+                            H2[kk].x = p.x;
+                            L2[kk].x = p.z;
+                        }
+                        if (e.y < 0.f && !(kk == P - 1 && K == NL - 1)) {
+                            H2[kk].y = p.y;
+                            L2[kk].y = p.w;
+                        }
                     }
                 }
             }
-            const float s = rho * ib;
-            float s1;
-            if constexpr (W == 1) {
-                s1 = __shfl_down_sync(kFull, s, 1);
-            } else {
-                x_s[K] = s;
-                __syncthreads();
-                s1 = x_s[K < NL - 1 ? K + 1 : K];
+            // ------------------------------------------------------------ result
+            double* V = vout + shape_row(sh, pde);
+#pragma unroll
+            for (int kk = 0; kk < P; ++kk) {
+                V[j0 + (kk == 0 ? 0 : P - kk)] = (double)H2[kk].x + (double)L2[kk].x;
+                V[j0 + P + kk] = (double)H2[kk].y + (double)L2[kk].y;
             }
-            if (K == NL - 1) s1 = 0.f;
-            y[0] = s;
-#pragma unroll
-            for (int i = 1; i < M; ++i) y[i] = fmaf(-s1, T(i, T_SR), fmaf(-s, T(i, T_SL), y[i]));
-            // V += d (float-float), then the early-exercise floor on nodes < N-1
-#pragma unroll
+        } else {
+            float H[M], Lo[M];  // V as float-float pairs, starting at the payoff
+    #pragma unroll
             for (int i = 0; i < M; ++i) {
-                ff_acc(H[i], Lo[i], y[i]);
-                if (amer && j0 + i < N - 1) {
-                    const float ph = T(i, T_PH), pl = T(i, T_PL);
-                    if ((H[i] - ph) + (Lo[i] - pl) < 0.f) {
-                        H[i] = ph;
-                        Lo[i] = pl;
+                const float2 p = PAY(i);
+                H[i] = p.x;
+                Lo[i] = p.y;
+            }
+
+            // ------------------------------------------------------------ time steps
+            for (int step = 1; run && step < TL; ++step) {
+                float Hm, Lm, Hp, Lp;
+                if constexpr (W == 1) {
+                    Hm = __shfl_up_sync(kFull, H[M - 1], 1);
+                    Lm = __shfl_up_sync(kFull, Lo[M - 1], 1);
+                    Hp = __shfl_down_sync(kFull, H[0], 1);
+                    Lp = __shfl_down_sync(kFull, Lo[0], 1);
+                } else {
+                    x_last[K] = make_float2(H[M - 1], Lo[M - 1]);
+                    x_first[K] = make_float2(H[0], Lo[0]);
+                    __syncthreads();
+                    const float2 pm = x_last[K > 0 ? K - 1 : 0], pp = x_first[K < NL - 1 ? K + 1 : 0];
+                    Hm = pm.x;
+                    Lm = pm.y;
+                    Hp = pp.x;
+                    Lp = pp.y;
+                }
+                if (K == 0) Hm = Lm = 0.f;
+                if (K == NL - 1) Hp = Lp = 0.f;
+                float y[M];
+                // residual r = dt A V from exact float-float differences
+    #pragma unroll
+                for (int i = 0; i < M; ++i) {
+                    const float hl = (i == 0) ? Hm : H[i - 1], ll = (i == 0) ? Lm : Lo[i - 1];
+                    const float hr = (i == M - 1) ? Hp : H[i + 1], lr = (i == M - 1) ? Lp : Lo[i + 1];
+                    const float hdu = hr - H[i], hdd = H[i] - hl, ldu = lr - Lo[i], ldd = Lo[i] - ll;
+                    const float Dup = hdu + ldu, Ddn = hdd + ldd, S = (hdu - hdd) + (ldu - ldd);
+                    if (kUni) {
+                        float r = c4u * (H[i] + Lo[i]);
+                        r = fmaf(c1u, S, r);
+                        r = fmaf(c2u, Dup, r);
+                        y[i] = fmaf(c3u, Ddn, r);
+                    } else {
+                        const float4 c = C(i);
+                        float r = c.w * (H[i] + Lo[i]);
+                        r = fmaf(c.x, S, r);
+                        r = fmaf(c.y, Dup, r);
+                        y[i] = fmaf(c.z, Ddn, r);
+                    }
+                }
+                if (kUni) {  // the one-sided boundary rows (no second difference)
+                    if (K == 0) y[0] = fmaf(c2b, (H[1] - H[0]) + (Lo[1] - Lo[0]), c4u * (H[0] + Lo[0]));
+                    if (K == NL - 1)
+                        y[M - 1] = fmaf(c3b, (H[M - 1] - H[M - 2]) + (Lo[M - 1] - Lo[M - 2]), c4u * (H[M - 1] + Lo[M - 1]));
+                }
+                interior_solve(y);
+                // separators: right-hand side, cyclic reduction, back to the interior
+                float ylp;
+                if constexpr (W == 1) {
+                    ylp = __shfl_up_sync(kFull, y[M - 1], 1);
+                } else {
+                    x_y[K] = y[M - 1];
+                    __syncthreads();
+                    ylp = x_y[K > 0 ? K - 1 : 0];
+                }
+                if (K == 0) ylp = 0.f;
+                float rho = y[0] - blaf * ylp - buaf * y[1];
+                if constexpr (W == 1) {
+    #pragma unroll
+                    for (int lv = 0; lv < kLevels; ++lv) {
+                        const int sg = 1 << lv;
+                        const float rm = __shfl_up_sync(kFull, rho, sg);
+                        const float rp = __shfl_down_sync(kFull, rho, sg);
+                        rho = rho - ka[lv] * rm - kc[lv] * rp;
+                    }
+                } else {
+                    float* cur = x_p0;
+                    float* nxt = x_p1;
+                    cur[K] = rho;
+                    __syncthreads();
+    #pragma unroll
+                    for (int lv = 0; lv < kLevels; ++lv) {
+                        const int sg = 1 << lv;
+                        const float rm = cur[K - sg >= 0 ? K - sg : K];
+                        const float rp = cur[K + sg < NL ? K + sg : K];
+                        rho = rho - ka[lv] * rm - kc[lv] * rp;  // ka, kc are 0 past the ends
+                        if (lv + 1 < kLevels) {
+                            nxt[K] = rho;
+                            __syncthreads();
+                            float* tmp = cur;
+                            cur = nxt;
+                            nxt = tmp;
+                        }
+                    }
+                }
+                const float s = rho * ib;
+                float s1;
+                if constexpr (W == 1) {
+                    s1 = __shfl_down_sync(kFull, s, 1);
+                } else {
+                    x_s[K] = s;
+                    __syncthreads();
+                    s1 = x_s[K < NL - 1 ? K + 1 : K];
+                }
+                if (K == NL - 1) s1 = 0.f;
+                y[0] = s;
+    #pragma unroll
+                for (int i = 1; i < M; ++i) {
+                    const float2 sp = SPK(i);
+                    y[i] = fmaf(-s1, sp.y, fmaf(-s, sp.x, y[i]));
+                }
+                // V += d (float-float), then the early-exercise floor on nodes < N-1
+    #pragma unroll
+                for (int i = 0; i < M; ++i) {
+                    ff_acc(H[i], Lo[i], y[i]);
+                    if (amer && j0 + i < N - 1) {
+                        const float2 p = PAY(i);
+                        if ((H[i] - p.x) + (Lo[i] - p.y) < 0.f) {
+                            H[i] = p.x;
+                            Lo[i] = p.y;
+                        }
                     }
                 }
             }
+            // ------------------------------------------------------------ result
+            double* V = vout + shape_row(sh, pde);
+    #pragma unroll
+            for (int i = 0; i < M; ++i)
+                if (j0 + i < N) V[j0 + i] = (double)H[i] + (double)Lo[i];
         }
-        // ------------------------------------------------------------ result
-        double* V = vout + shape_row(sh, pde);
-#pragma unroll
-        for (int i = 0; i < M; ++i)
-            if (j0 + i < N) V[j0 + i] = (double)H[i] + (double)Lo[i];
         if (K == 0) pde_status[pde] = st;
     }
 }
@@ -552,7 +802,8 @@ int& per_sm_fp32()
 template <int M, bool kUni, int W>
 constexpr size_t fp32_smem()
 {
-    return ((size_t)M * f32_fields<kUni>() * 32 * W + (kUni ? (size_t)M * kSharedFields * 2 : 0)) * sizeof(float) +
+    return ((size_t)M * f32_fields<kUni>() * 32 * W + (kUni ? (size_t)M * kSharedFields * 2 : 0) +
+            (size_t)f32_pair_floats<M, kUni, W>()) * sizeof(float) +
            f32_xchg_bytes<W>();
 }
 

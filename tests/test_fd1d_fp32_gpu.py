@@ -116,3 +116,19 @@ def test_32768x1024_full_size_vs_fp64(ctx):
     assert (st == 0).all()
     err = np.abs(p32 - p64)
     assert err.max() <= ABS_TOL, (err.max(), int(err.argmax()))
+
+
+@pytest.mark.parametrize("theta", [0.5, 0.75])
+@pytest.mark.parametrize("x_dim", [128, 256, 512, 1024])
+def test_uniform_full_lane_grids(ctx, x_dim, theta):
+    """Uniform grids of 32 x 2^k nodes run the packed-pair step (nodes P-k and P+k of
+    a lane in one float2, P = nodes per lane / 2): 4, 8, 16 and 32 nodes per lane, a
+    mix of American and European puts and calls, against the oracle."""
+    import portfolio
+
+    o = portfolio.american_portfolio(96, seed=31)
+    o["e"][1::3] = 0
+    o["w"][::2] = -o["w"][::2]
+    p, st = price32(ctx, o, t_dim=300, x_dim=x_dim, scale=5.0, density=math.inf, theta=theta)
+    want = oracle(o, t_dim=300, x_dim=x_dim, scale=5.0, density=math.inf, theta=theta)
+    assert (st == 0).all() and np.max(np.abs(p - want)) <= ABS_TOL
