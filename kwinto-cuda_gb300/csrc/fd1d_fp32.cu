@@ -20,11 +20,19 @@
 //
 // Solve of B d = r (N_p = 32 W M nodes, lane k owns nodes kM .. kM+M-1):
 //   * node kM is a separator s_k; nodes kM+1 .. kM+M-1 are lane k's interior;
-//   * interior:  d_I = y - s_k L - s_{k+1} R,  y = B_I^-1 r_I  (local Thomas,
+//   * interior:  d_I = y - s_k L - s_{k+1} R,  y = B_I^-1 r_I  (a twisted
+//     factorisation: eliminated from both ends towards the lane's pivot node kM+M/2;
 //     factors and the spikes L, R precomputed once per PDE);
 //   * separators: a 32 W-unknown tridiagonal system, solved by parallel cyclic
 //     reduction (5 + log2 W levels, multipliers precomputed).
 // B, dt and the grid do not change between steps, so all factors are computed once.
+//
+// Packed pairs.  Each step runs on float2 values with the packed FP32 instructions
+// of sm_100 and later (__fadd2_rn, __fmul2_rn, __ffma2_rn: two FP32 operations per
+// issued instruction).  A lane's nodes are paired around its pivot P = M/2: nodes P-k
+// and P+k share a float2.  The residual, the spike correction and the update are
+// per-node work, so any pairing packs them; this one also packs the twisted solve,
+// whose two elimination chains walk P-k and P+k in step.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -36,20 +44,25 @@ namespace kwg {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-// Tables per node, grouped by the step that reads them so that each group is one
-// vector load: the payoff pair (PH, PL); the forward-elimination pair (L, ID); U of
-// the back substitution; the two spike values (SL, SR); and, on non-uniform grids,
-// the residual coefficients (C1, C2, C3, C4).  Per-lane groups are laid out
-// [node-in-lane][lane] (consecutive lanes, conflict-free).  On a uniform grid
-// without padded nodes the interior rows of B are the same at every node, so
-//   * the residual coefficients c1..c4 live in registers;
-//   * every lane but the last has the same interior block B_I, hence the same LU
-//     factors and spikes: (L, ID), U and (SL, SR) are kept once for the group plus
-//     once for the last lane (whose block holds the boundary row), [node][2], read
-//     as broadcasts; only the payoff pair stays per lane.
+// Tables, by slot: a lane's M nodes are paired around its pivot row P = M/2 -- slot k
+// (k = 1 .. P-1) holds nodes a = P-k and b = P+k, slot 0 holds node 0 (the lane's
+// separator) and node P -- so that each step runs on packed FP32 pairs (below).
+//   PP  (hi_a, hi_b, lo_a, lo_b)  the payoff as float-float pairs      per lane
+//   F0  (l_a, l_b, id_a, id_b)    twisted elimination, inverse pivots
+//   F1  (u_a, u_b, sl_a, sl_b)    back substitution, left spike
+//   F2  (sr_a, sr_b)              right spike
+//   C0  (c1_a, c1_b, c4_a, c4_b), C1 (c2_a, -c3_b, c3_a, -c2_b)   residual coefficients
+// Per-lane groups are laid out [slot][lane] (consecutive lanes, conflict-free).  On a
+// uniform grid without padded nodes the interior rows of B are the same at every
+// node, so
+//   * the residual coefficients c1..c4 live in registers (no C0, C1);
+//   * every lane but the last has the same interior block B_I, hence the same
+//     factors and spikes: F0, F1, F2 are kept once for the group plus once for the
+//     last lane (whose block holds the boundary row), [slot][2], read as broadcasts;
+//     only the payoff stays per lane.
 template <bool kUni>
 __host__ __device__ constexpr int f32_fields() { return kUni ? 2 : 11; }  // per-lane floats per node
-constexpr int kSharedFields = 5;                                          // L, ID, U, SL, SR
+constexpr int kSharedFields = 5;                                          // l, id, u, sl, sr
 
 struct FF {
     float hi, lo;
@@ -93,18 +106,6 @@ __device__ __forceinline__ void ff_acc2(float2& h, float2& l, float2 d)
 
 }  // namespace
 
-// Uniform grids, one warp per PDE, at least 4 nodes per lane: the step runs on packed
-// FP32 pairs.  A lane's nodes are paired around its pivot row P = M/2 -- slot k holds
-// nodes (P-k, P+k) for k = 1 .. P-1, slot 0 nodes (0, P) -- so that the two chains of
-// the twisted interior solve, which walk P-k and P+k in step, are the two halves of
-// one packed operation, and so are the per-node residual, spike and update.  The
-// tables are repacked by slot after the setup: the payoff as (hi(P-k), hi(P+k),
-// lo(P-k), lo(P+k)) per lane, the shared factors as three float4 per slot.
-template <int M, bool kUni, int W>
-__host__ __device__ constexpr bool f32_paired() { return kUni && W == 1 && M >= 4; }
-template <int M, bool kUni, int W>
-__host__ __device__ constexpr int f32_pair_floats() { return f32_paired<M, kUni, W>() ? 2 * M * 32 + 12 * M : 0; }
-
 // Shared-memory bytes of the lane-exchange area of a W-warp PDE group (W > 1).
 template <int W>
 __host__ __device__ constexpr int f32_xchg_bytes()
@@ -122,57 +123,85 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
     constexpr int kF = f32_fields<kUni>();
     constexpr int NL = 32 * W;
     constexpr int kLevels = W == 1 ? 5 : W == 2 ? 6 : W == 4 ? 7 : 8;  // log2 of the lanes
-    constexpr int kPivot = M / 2;  // pivot row of the twisted interior factorisation
+    constexpr int P = M / 2;  // pivot row of the twisted interior factorisation
     static_assert(M % 2 == 0, "an even number of nodes per lane: as many rows above the pivot as below");
     static_assert(W == 1 || W == 2 || W == 4 || W == 8, "1, 2, 4 or 8 warps per PDE");
-    // Tables: non-uniform grids C [M][NL] float4, then PAY, LID, SPK [M][NL] float2,
-    // then U [M][NL]; uniform grids PAY [M][NL] float2, then the shared factors LID,
-    // SPK [M][2] float2 and U [M][2]; then the exchange area (W > 1).
+    // Tables (floats): non-uniform grids C0, C1, F0, F1 [P][NL] float4, F2 [P][NL] float2,
+    // PP [P][NL] float4; uniform grids PP [P][NL] float4, F0, F1 [P][2] float4, F2 [P][2]
+    // float2; then the exchange area (W > 1).
     extern __shared__ float tab[];
     const int k = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int K = threadIdx.x;  // lane of the PDE group
     constexpr int kTabFloats = M * kF * NL + (kUni ? M * kSharedFields * 2 : 0);
-    // per-lane groups at [i * NL + K]; the uniform grid's shared groups at [i * 2 + c]
-    // with c = 1 for the last lane only, computed arithmetically ((K + 1) / NL with NL
-    // a power of two) so that the loads stay single loads from one base address
-    constexpr int kLane0 = kUni ? 0 : 4 * M * NL;  // floats before PAY
-    float2* const pay = reinterpret_cast<float2*>(tab + kLane0) + K;
-    float4* const cof = reinterpret_cast<float4*>(tab) + K;
-    constexpr int kStride = kUni ? 2 : NL;  // elements per node of the factor groups
+    // per-lane groups at [slot * NL + K]; the uniform grid's shared groups at
+    // [slot * 2 + c] with c = 1 for the last lane only, computed arithmetically
+    // ((K + 1) / NL with NL a power of two) so that the loads stay single loads
+    constexpr int kStride = kUni ? 2 : NL;  // elements per slot of the factor groups
+    constexpr int kF0 = kUni ? 2 * M * NL : 4 * M * NL;
+    constexpr int kPP = kUni ? 0 : 9 * M * NL;
     const int own = kUni ? (K + 1) / NL : K;
-    float2* const lid = reinterpret_cast<float2*>(tab + kLane0 + 2 * M * NL) + own;
-    float2* const spk = lid + M * kStride;
-    float* const ufac = reinterpret_cast<float*>(tab + kLane0 + 2 * M * NL + 4 * M * kStride) + own;
+    float4* const C0t = reinterpret_cast<float4*>(tab) + K;
+    float4* const C1t = reinterpret_cast<float4*>(tab + 2 * M * NL) + K;
+    float4* const F0t = reinterpret_cast<float4*>(tab + kF0) + own;
+    float4* const F1t = F0t + P * kStride;
+    float2* const F2t = reinterpret_cast<float2*>(tab + kF0 + 4 * M * kStride) + own;
+    float4* const PPt = reinterpret_cast<float4*>(tab + kPP) + K;
     // uniform grid: lane 0 writes the group's factors, the last lane its own
     const bool writer = !kUni || K == 0 || K == NL - 1;
-    auto PAY = [&](int i) -> float2& { return pay[i * NL]; };
-    auto LID = [&](int i) -> float2& { return lid[i * kStride]; };
-    auto SPK = [&](int i) -> float2& { return spk[i * kStride]; };
-    auto U = [&](int i) -> float& { return ufac[i * kStride]; };
-    auto C = [&](int i) -> float4& { return cof[i * NL]; };
+    // node i of the lane -> its slot and component (0: node P-k or node 0; 1: P+k or P)
+    auto slot_of = [](int i) { return i == 0 ? 0 : (i < P ? P - i : i - P); };
+    auto comp_of = [](int i) { return i >= P ? 1 : 0; };
+    auto part = [](float4& q, int f) -> float& { return reinterpret_cast<float*>(&q)[f]; };
+    auto PH = [&](int i) -> float& { return part(PPt[slot_of(i) * NL], comp_of(i)); };
+    auto PL = [&](int i) -> float& { return part(PPt[slot_of(i) * NL], 2 + comp_of(i)); };
+    auto L = [&](int i) -> float& { return part(F0t[slot_of(i) * kStride], comp_of(i)); };
+    auto ID = [&](int i) -> float& { return part(F0t[slot_of(i) * kStride], 2 + comp_of(i)); };
+    auto U = [&](int i) -> float& { return part(F1t[slot_of(i) * kStride], comp_of(i)); };
+    auto SL = [&](int i) -> float& { return part(F1t[slot_of(i) * kStride], 2 + comp_of(i)); };
+    auto SR = [&](int i) -> float& {
+        float2& q = F2t[slot_of(i) * kStride];
+        return comp_of(i) ? q.y : q.x;
+    };
+    // residual coefficients of node i; for the b node of a slot c2 and c3 are stored
+    // negated and swapped, which lets one packed FMA serve both components (below)
+    auto set_c = [&](int i, float c1, float c2, float c3, float c4) {
+        float4& q0 = C0t[slot_of(i) * NL];
+        float4& q1 = C1t[slot_of(i) * NL];
+        if (comp_of(i) == 0) {
+            q0.x = c1;
+            q0.z = c4;
+            q1.x = c2;
+            q1.z = c3;
+        } else {
+            q0.y = c1;
+            q0.w = c4;
+            q1.w = -c2;
+            q1.y = -c3;
+        }
+    };
     // B_I^-1 v in place on nodes 1 .. M-1 by a twisted factorisation: eliminate from
-    // both ends towards node kPivot (two independent chains), solve that row, then
-    // substitute back outward (two chains again).  Tables: rows above the pivot
-    // (L, ID) = (l_i, 1/d_i), U = bu_i/d_i of the top-down LU; rows below it
-    // (m_i, 1/e_i), bl_i/e_i of the bottom-up elimination; the pivot row (l_P, 1/gamma)
-    // and U = m_P.
+    // both ends towards node P (two independent chains), solve that row, then
+    // substitute back outward (two chains again).  Factors: rows above the pivot
+    // (l, id, u) = (l_i, 1/d_i, bu_i/d_i) of the top-down LU; rows below it
+    // (m_i, 1/e_i, bl_i/e_i) of the bottom-up elimination; the pivot row
+    // (l_P, 1/gamma, m_P).  Scalar form, used by the setup for the spikes; the steps
+    // run the same operations on packed pairs.
     auto interior_solve = [&](float (&v)[M]) {
         float f = 0.f, g = 0.f;
 #pragma unroll
-        for (int jj = 0; jj < kPivot - 1; ++jj) {
+        for (int jj = 0; jj < P - 1; ++jj) {
             const int it = 1 + jj, ib = M - 1 - jj;
-            f = fmaf(-LID(it).x, f, v[it]);
+            f = fmaf(-L(it), f, v[it]);
             v[it] = f;
-            g = fmaf(-LID(ib).x, g, v[ib]);
+            g = fmaf(-L(ib), g, v[ib]);
             v[ib] = g;
         }
-        const float2 lp = LID(kPivot);
-        v[kPivot] = fmaf(-U(kPivot), g, fmaf(-lp.x, f, v[kPivot])) * lp.y;
+        v[P] = fmaf(-U(P), g, fmaf(-L(P), f, v[P])) * ID(P);
 #pragma unroll
-        for (int jj = 0; jj < kPivot - 1; ++jj) {
-            const int it = kPivot - 1 - jj, ib = kPivot + 1 + jj;
-            v[it] = fmaf(-U(it), v[it + 1], v[it] * LID(it).y);
-            v[ib] = fmaf(-U(ib), v[ib - 1], v[ib] * LID(ib).y);
+        for (int jj = 0; jj < P - 1; ++jj) {
+            const int it = P - 1 - jj, ib = P + 1 + jj;
+            v[it] = fmaf(-U(it), v[it + 1], v[it] * ID(it));
+            v[ib] = fmaf(-U(ib), v[ib - 1], v[ib] * ID(ib));
         }
     };
     const int j0 = K * M;
@@ -267,8 +296,9 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
                     // the payoff is exactly 0 on the out-of-the-money side: skip exp there
                     if ((w < 0) ? (x0 < 0.) : (x0 > 0.)) p = split(payoff(w, x0));
                 }
-                if (!kUni) C(i) = make_float4(c1, c2, c3, c4);
-                PAY(i) = make_float2(p.hi, p.lo);
+                if (!kUni) set_c(i, c1, c2, c3, c4);
+                PH(i) = p.hi;
+                PL(i) = p.lo;
                 if (i == 0) {
                     bla = bl;
                     ba = bb;
@@ -280,11 +310,12 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
                     if (!(d != 0.) || !isfinite(d)) st = st == KWG_STATUS_OK ? KWG_STATUS_SOLVER : st;
                     const double idd = 1. / d;
                     const double u = bu * idd;
-                    if (writer && i < kPivot) {
-                        LID(i) = make_float2((float)l, (float)idd);
+                    if (writer && i < P) {
+                        L(i) = (float)l;
+                        ID(i) = (float)idd;
                         U(i) = (float)u;
                     }
-                    if (i == kPivot) {
+                    if (i == P) {
                         bl_piv = bl;
                         b_piv = bb;
                         bu_piv = bu;
@@ -320,8 +351,8 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
             R1 = Rlast * pr;
             bl_first_f = bl_first;
         }
-        // Bottom part of the twisted factorisation of B_I (rows M-1 .. kPivot+1,
-        // eliminating upward from the lane's last node) and the pivot row kPivot:
+        // Bottom part of the twisted factorisation of B_I (rows M-1 .. P+1,
+        // eliminating upward from the lane's last node) and the pivot row P:
         //   e_i = b_i - m_i bl_{i+1},  m_i = bu_i / e_{i+1}  (m_{M-1} = 0),
         //   gamma = b_P - l_P bu_{P-1} - m_P bl_{P+1}.
         if (writer) {
@@ -329,7 +360,7 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
             const int jt = j0 + M - 1;
             double xp = (jt + 1 < N) ? g.x(jt + 1) : 0., x0 = (jt < N) ? g.x(jt) : 0.;
 #pragma unroll 1
-            for (int i = M - 1; i > kPivot; --i) {
+            for (int i = M - 1; i > P; --i) {
                 const int j = j0 + i;
                 const double xm = (j - 1 < N) ? g.x(j - 1) : 0.;
                 double bl = 0., bb = 1., bu = 0.;
@@ -343,19 +374,21 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
                 const double e = (i == M - 1) ? bb : bb - m * bl_next;
                 if (!(e != 0.) || !isfinite(e)) st = st == KWG_STATUS_OK ? KWG_STATUS_SOLVER : st;
                 const double ie = 1. / e;
-                LID(i) = make_float2((float)m, (float)ie);
+                L(i) = (float)m;
+                ID(i) = (float)ie;
                 U(i) = (float)(bl * ie);
                 e_next = e;
                 bl_next = bl;
                 xp = x0;
                 x0 = xm;
             }
-            const double m_piv = (kPivot == M - 1) ? 0. : bu_piv / e_next;
+            const double m_piv = (P == M - 1) ? 0. : bu_piv / e_next;
             const double gam = b_piv - l_piv * bu_above - m_piv * bl_next;
             if (!(gam != 0.) || !isfinite(gam)) st = st == KWG_STATUS_OK ? KWG_STATUS_SOLVER : st;
             (void)bl_piv;
-            LID(kPivot) = make_float2((float)l_piv, (float)(1. / gam));
-            U(kPivot) = (float)m_piv;
+            L(P) = (float)l_piv;
+            ID(P) = (float)(1. / gam);
+            U(P) = (float)m_piv;
             // spikes L = B_I^-1 (bl_1 e_1) and R = B_I^-1 (bu_{M-1} e_{M-1}), by the
             // same FP32 solve the steps use
             float v[M];
@@ -364,13 +397,13 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
             v[1] = (float)bl_first_f;
             interior_solve(v);
 #pragma unroll
-            for (int i = 1; i < M; ++i) SPK(i).x = v[i];
+            for (int i = 1; i < M; ++i) SL(i) = v[i];
 #pragma unroll
             for (int i = 0; i < M; ++i) v[i] = 0.f;
             v[M - 1] = (float)bu_last_f;
             interior_solve(v);
 #pragma unroll
-            for (int i = 1; i < M; ++i) SPK(i).y = v[i];
+            for (int i = 1; i < M; ++i) SR(i) = v[i];
         }
         // separator system (FP64) and its cyclic-reduction multipliers (stored FP32)
         float ka[kLevels], kc[kLevels], ib;
@@ -454,126 +487,160 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
             else
                 __syncthreads();
         }
-        if constexpr (f32_paired<M, kUni, W>()) {
-            constexpr int P = M / 2;
-            // repack the tables by slot (node P-k and P+k; slot 0: node 0 and the pivot P)
-            float4* const ppay = reinterpret_cast<float4*>(tab + kTabFloats) + K;          // [P][NL]
-            float4* const pfac = reinterpret_cast<float4*>(tab + kTabFloats + 4 * P * NL) + 3 * own;  // [P][2][3]
+        // ------------------------------------------------------------ time steps
+        // V as float-float pairs by slot, starting at the payoff
+        float2 H2[P], L2[P];
 #pragma unroll
-            for (int kk = 0; kk < P; ++kk) {
-                const float2 pa = PAY(kk == 0 ? 0 : P - kk), pb = PAY(P + kk);
-                ppay[kk * NL] = make_float4(pa.x, pb.x, pa.y, pb.y);
+        for (int kk = 0; kk < P; ++kk) {
+            const float4 p = PPt[kk * NL];
+            H2[kk] = make_float2(p.x, p.y);
+            L2[kk] = make_float2(p.z, p.w);
+        }
+        // Residual coefficients by component.  Slot k's a node (P-k) has the upward
+        // difference D_k.x and the downward D_(k+1).x; its b node (P+k) the upward
+        // -D_(k+1).y and the downward -D_k.y (D_k = V_(k-1) - V_k of the slots, below),
+        // so (c2_a, -c3_b) multiplies D_k and (c3_a, -c2_b) multiplies D_(k+1).
+        const float2 c4u2 = make_float2(c4u, c4u), c1u2 = make_float2(c1u, c1u);
+        const float2 c23u = make_float2(c2u, -c3u), c32u = make_float2(c3u, -c2u);
+        // the early-exercise floor applies on nodes < N-1: on a grid of full lanes every
+        // node but the last lane's node M-1 (slot P-1 .y); elsewhere the lane's nodes
+        // below lim
+        const int lim = N - 1 - j0;
+        for (int step = 1; run && step < TL; ++step) {
+            // neighbours across lanes: node -1 is lane K-1's node M-1 (slot P-1 .y), node
+            // M is lane K+1's node 0 (slot 0 .x)
+            float Hm, Lm, Hp, Lp;
+            if constexpr (W == 1) {
+                Hm = __shfl_up_sync(kFull, H2[P - 1].y, 1);
+                Lm = __shfl_up_sync(kFull, L2[P - 1].y, 1);
+                Hp = __shfl_down_sync(kFull, H2[0].x, 1);
+                Lp = __shfl_down_sync(kFull, L2[0].x, 1);
+            } else {
+                x_last[K] = make_float2(H2[P - 1].y, L2[P - 1].y);
+                x_first[K] = make_float2(H2[0].x, L2[0].x);
+                __syncthreads();
+                const float2 pm = x_last[K > 0 ? K - 1 : 0], pp = x_first[K < NL - 1 ? K + 1 : 0];
+                Hm = pm.x;
+                Lm = pm.y;
+                Hp = pp.x;
+                Lp = pp.y;
             }
-            if (writer) {
+            if (K == 0) Hm = Lm = 0.f;
+            if (K == NL - 1) Hp = Lp = 0.f;
+            // differences of consecutive slots, D_k = V_(k-1) - V_k (k = 1 .. P), with the
+            // pivot in both components before slot 1 and (node 0, node M) after slot P-1:
+            // .x = V(P-k+1) - V(P-k), .y = V(P+k-1) - V(P+k); hi and lo parts each exact
+            auto diff = [&](int kk, float2& dh, float2& dl) {
+                const float2 hu = kk == 1 ? make_float2(H2[0].y, H2[0].y) : H2[kk - 1];
+                const float2 lu = kk == 1 ? make_float2(L2[0].y, L2[0].y) : L2[kk - 1];
+                const float2 hd = kk == P ? make_float2(H2[0].x, Hp) : H2[kk];
+                const float2 ld = kk == P ? make_float2(L2[0].x, Lp) : L2[kk];
+                dh = sub2(hu, hd);
+                dl = sub2(lu, ld);
+            };
+            // residual r = dt A V on the slots 1 .. P-1, two nodes per operation
+            float2 y2[P];
+            float2 dh1, dl1;
+            diff(1, dh1, dl1);
+            float2 dh = dh1, dl = dl1, d = __fadd2_rn(dh1, dl1);
 #pragma unroll
-                for (int kk = 0; kk < P; ++kk) {
-                    const int na = kk == 0 ? P : P - kk, nb = P + kk;  // slot 0: the pivot row twice
-                    const float2 la = LID(na), lb = LID(nb), sa = SPK(na), sb = SPK(nb);
-                    pfac[kk * 6 + 0] = make_float4(la.x, lb.x, la.y, lb.y);
-                    pfac[kk * 6 + 1] = make_float4(U(na), U(nb), sa.x, sb.x);
-                    pfac[kk * 6 + 2] = make_float4(sa.y, sb.y, 0.f, 0.f);
+            for (int kk = 1; kk < P; ++kk) {
+                float2 dhn, dln;
+                diff(kk + 1, dhn, dln);
+                const float2 dn = __fadd2_rn(dhn, dln);
+                const float2 S = __fadd2_rn(sub2(dh, dhn), sub2(dl, dln));
+                float2 c1v = c1u2, c4v = c4u2, c23 = c23u, c32 = c32u;
+                if constexpr (!kUni) {
+                    const float4 q0 = C0t[kk * NL], q1 = C1t[kk * NL];
+                    c1v = make_float2(q0.x, q0.y);
+                    c4v = make_float2(q0.z, q0.w);
+                    c23 = make_float2(q1.x, q1.y);
+                    c32 = make_float2(q1.z, q1.w);
                 }
+                float2 r = __fmul2_rn(c4v, __fadd2_rn(H2[kk], L2[kk]));
+                r = __ffma2_rn(c1v, S, r);
+                r = __ffma2_rn(c23, d, r);
+                y2[kk] = __ffma2_rn(c32, dn, r);
+                dh = dhn;
+                dl = dln;
+                d = dn;
             }
-            __syncwarp();
-            float2 H2[P], L2[P];  // V as float-float pairs by slot, starting at the payoff
-#pragma unroll
-            for (int kk = 0; kk < P; ++kk) {
-                const float4 p = ppay[kk * NL];
-                H2[kk] = make_float2(p.x, p.y);
-                L2[kk] = make_float2(p.z, p.w);
+            // ... and on slot 0, node by node: the pivot P and the separator 0
+            float c1a = c1u, c2a = c2u, c3a = c3u, c4a = c4u, c1b = c1u, c2b_ = c2u, c3b_ = c3u, c4b = c4u;
+            if constexpr (!kUni) {
+                const float4 q0 = C0t[0], q1 = C1t[0];
+                c1a = q0.x;
+                c4a = q0.z;
+                c2a = q1.x;
+                c3a = q1.z;
+                c1b = q0.y;
+                c4b = q0.w;
+                c2b_ = -q1.w;
+                c3b_ = -q1.y;
             }
-            // residual coefficients by component: .x of slot k is node P-k, whose upward
-            // difference is D_k.x; .y is node P+k, whose upward difference is -D_(k+1).y
-            const float2 c4v = make_float2(c4u, c4u), c1v = make_float2(c1u, c1u);
-            const float2 c23 = make_float2(c2u, -c3u), c32 = make_float2(c3u, -c2u);
-            for (int step = 1; run && step < TL; ++step) {
-                float Hm = __shfl_up_sync(kFull, H2[P - 1].y, 1);
-                float Lm = __shfl_up_sync(kFull, L2[P - 1].y, 1);
-                float Hp = __shfl_down_sync(kFull, H2[0].x, 1);
-                float Lp = __shfl_down_sync(kFull, L2[0].x, 1);
-                if (K == 0) Hm = Lm = 0.f;
-                if (K == NL - 1) Hp = Lp = 0.f;
-                // differences of consecutive slots, D_k = V_(k-1) - V_k (k = 1 .. P), with the
-                // pivot in both components before slot 1 and (node 0, node M) after slot P-1:
-                // .x = V(P-k+1) - V(P-k), .y = V(P+k-1) - V(P+k), hi and lo parts exactly
-                auto diff = [&](int kk, float2& dh, float2& dl) {
-                    const float2 hu = kk == 1 ? make_float2(H2[0].y, H2[0].y) : H2[kk - 1];
-                    const float2 lu = kk == 1 ? make_float2(L2[0].y, L2[0].y) : L2[kk - 1];
-                    const float2 hd = kk == P ? make_float2(H2[0].x, Hp) : H2[kk];
-                    const float2 ld = kk == P ? make_float2(L2[0].x, Lp) : L2[kk];
-                    dh = sub2(hu, hd);
-                    dl = sub2(lu, ld);
-                };
-                float2 y2[P];
-                float2 dh1, dl1, dhP, dlP;
-                diff(1, dh1, dl1);
-                float2 dh = dh1, dl = dl1, d = __fadd2_rn(dh1, dl1);
-#pragma unroll
-                for (int kk = 1; kk < P; ++kk) {
-                    float2 dhn, dln;
-                    diff(kk + 1, dhn, dln);
-                    const float2 dn = __fadd2_rn(dhn, dln);
-                    const float2 S = __fadd2_rn(sub2(dh, dhn), sub2(dl, dln));
-                    float2 r = __fmul2_rn(c4v, __fadd2_rn(H2[kk], L2[kk]));
-                    r = __ffma2_rn(c1v, S, r);
-                    r = __ffma2_rn(c23, d, r);
-                    y2[kk] = __ffma2_rn(c32, dn, r);
-                    dh = dhn;
-                    dl = dln;
-                    d = dn;
-                }
-                dhP = dh;
-                dlP = dl;
-                // the pivot P and the separator 0, node by node
-                float yP, y0;
-                {
-                    const float hdu = -dh1.y, hdd = dh1.x, ldu = -dl1.y, ldd = dl1.x;
-                    const float Dup = hdu + ldu, Ddn = hdd + ldd, S = (hdu - hdd) + (ldu - ldd);
-                    float r = c4u * (H2[0].y + L2[0].y);
-                    r = fmaf(c1u, S, r);
-                    r = fmaf(c2u, Dup, r);
-                    yP = fmaf(c3u, Ddn, r);
-                }
-                {
-                    const float hdu = dhP.x, hdd = H2[0].x - Hm, ldu = dlP.x, ldd = L2[0].x - Lm;
-                    const float Dup = hdu + ldu, Ddn = hdd + ldd, S = (hdu - hdd) + (ldu - ldd);
-                    float r = c4u * (H2[0].x + L2[0].x);
-                    r = fmaf(c1u, S, r);
-                    r = fmaf(c2u, Dup, r);
-                    y0 = fmaf(c3u, Ddn, r);
-                    // the one-sided boundary rows (no second difference): node 0 of the first
-                    // lane, node M-1 (slot P-1 .y) of the last
-                    if (K == 0) y0 = fmaf(c2b, hdu + ldu, c4u * (H2[0].x + L2[0].x));
-                }
-                if (K == NL - 1) {
-                    const float2 dm = sub2(H2[P - 1], H2[P - 2 > 0 ? P - 2 : 0]);
-                    const float2 lm = sub2(L2[P - 1], L2[P - 2 > 0 ? P - 2 : 0]);
-                    // node M-1 minus node M-2 (for P = 2 node M-2 is the pivot, slot 0 .y)
+            float yP, y0;
+            {
+                const float hdu = -dh1.y, hdd = dh1.x, ldu = -dl1.y, ldd = dl1.x;
+                const float Dup = hdu + ldu, Ddn = hdd + ldd, S = (hdu - hdd) + (ldu - ldd);
+                float r = c4b * (H2[0].y + L2[0].y);
+                r = fmaf(c1b, S, r);
+                r = fmaf(c2b_, Dup, r);
+                yP = fmaf(c3b_, Ddn, r);
+            }
+            {
+                const float hdu = dh.x, hdd = H2[0].x - Hm, ldu = dl.x, ldd = L2[0].x - Lm;  // dh = D_P
+                const float Dup = hdu + ldu, Ddn = hdd + ldd, S = (hdu - hdd) + (ldu - ldd);
+                float r = c4a * (H2[0].x + L2[0].x);
+                r = fmaf(c1a, S, r);
+                r = fmaf(c2a, Dup, r);
+                y0 = fmaf(c3a, Ddn, r);
+                // uniform grids: the one-sided boundary rows (no second difference) --
+                // node 0 of the first lane, node M-1 of the last
+                if (kUni && K == 0) y0 = fmaf(c2b, hdu + ldu, c4u * (H2[0].x + L2[0].x));
+            }
+            if (kUni && K == NL - 1) {
+                if constexpr (P == 1) {
+                    yP = fmaf(c3b, dh1.x + dl1.x, c4u * (H2[0].y + L2[0].y));  // node 1 = the pivot
+                } else {
+                    // node M-1 minus node M-2 (slot P-2 .y; for P = 2 the pivot, slot 0 .y)
+                    const float2 dm = sub2(H2[P - 1], H2[P - 2]), lm = sub2(L2[P - 1], L2[P - 2]);
                     y2[P - 1].y = fmaf(c3b, dm.y + lm.y, c4u * (H2[P - 1].y + L2[P - 1].y));
                 }
-                // interior: twisted elimination, both chains in one packed operation ...
-                float2 F = make_float2(0.f, 0.f);
+            }
+            // interior: twisted elimination, the two chains in one packed operation ...
+            float2 F = make_float2(0.f, 0.f);
 #pragma unroll
-                for (int kk = P - 1; kk >= 1; --kk) {
-                    const float4 f0 = pfac[kk * 6];
-                    F = __ffma2_rn(make_float2(-f0.x, -f0.y), F, y2[kk]);
-                    y2[kk] = F;
-                }
-                // ... the pivot row ...
-                const float4 fp0 = pfac[0], fp1 = pfac[1], fp2 = pfac[2];
-                yP = fmaf(-fp1.y, F.y, fmaf(-fp0.y, F.x, yP)) * fp0.w;
-                // ... and the back substitution outward
-                float2 X = make_float2(yP, yP);
+            for (int kk = P - 1; kk >= 1; --kk) {
+                const float4 f0 = F0t[kk * kStride];
+                F = __ffma2_rn(make_float2(-f0.x, -f0.y), F, y2[kk]);
+                y2[kk] = F;
+            }
+            // ... the pivot row (F holds f_(P-1) and g_(P+1); 0 when P = 1) ...
+            const float4 fp0 = F0t[0], fp1 = F1t[0];
+            const float2 fp2 = F2t[0];
+            yP = fmaf(-fp1.y, F.y, fmaf(-fp0.y, F.x, yP)) * fp0.w;
+            // ... and the back substitution outward
+            float2 X = make_float2(yP, yP);
 #pragma unroll
-                for (int kk = 1; kk < P; ++kk) {
-                    const float4 f0 = pfac[kk * 6], f1 = pfac[kk * 6 + 1];
-                    X = __ffma2_rn(make_float2(-f1.x, -f1.y), X, __fmul2_rn(y2[kk], make_float2(f0.z, f0.w)));
-                    y2[kk] = X;
-                }
-                // separators: right-hand side, cyclic reduction, back to the interior
-                float ylp = __shfl_up_sync(kFull, y2[P - 1].y, 1);  // lane K-1's node M-1
-                if (K == 0) ylp = 0.f;
-                float rho = y0 - blaf * ylp - buaf * y2[P - 1].x;  // node 1 is slot P-1 .x
+            for (int kk = 1; kk < P; ++kk) {
+                const float4 f0 = F0t[kk * kStride], f1 = F1t[kk * kStride];
+                X = __ffma2_rn(make_float2(-f1.x, -f1.y), X, __fmul2_rn(y2[kk], make_float2(f0.z, f0.w)));
+                y2[kk] = X;
+            }
+            // separators: right-hand side, cyclic reduction, back to the interior
+            const float y_last = P == 1 ? yP : y2[P - 1].y;   // node M-1
+            const float y_first = P == 1 ? yP : y2[P - 1].x;  // node 1
+            float ylp;
+            if constexpr (W == 1) {
+                ylp = __shfl_up_sync(kFull, y_last, 1);
+            } else {
+                x_y[K] = y_last;
+                __syncthreads();
+                ylp = x_y[K > 0 ? K - 1 : 0];
+            }
+            if (K == 0) ylp = 0.f;
+            float rho = y0 - blaf * ylp - buaf * y_first;
+            if constexpr (W == 1) {
 #pragma unroll
                 for (int lv = 0; lv < kLevels; ++lv) {
                     const int sg = 1 << lv;
@@ -581,171 +648,72 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
                     const float rp = __shfl_down_sync(kFull, rho, sg);
                     rho = rho - ka[lv] * rm - kc[lv] * rp;
                 }
-                const float sv = rho * ib;
-                float s1 = __shfl_down_sync(kFull, sv, 1);
-                if (K == NL - 1) s1 = 0.f;
-                const float2 ms = make_float2(-sv, -sv), ms1 = make_float2(-s1, -s1);
+            } else {
+                float* cur = x_p0;
+                float* nxt = x_p1;
+                cur[K] = rho;
+                __syncthreads();
 #pragma unroll
-                for (int kk = 1; kk < P; ++kk) {
-                    const float4 f1 = pfac[kk * 6 + 1], f2 = pfac[kk * 6 + 2];
-                    y2[kk] = __ffma2_rn(ms1, make_float2(f2.x, f2.y), __ffma2_rn(ms, make_float2(f1.z, f1.w), y2[kk]));
-                }
-                y2[0] = make_float2(sv, fmaf(-s1, fp2.x, fmaf(-sv, fp1.z, yP)));
-                // V += d (float-float), then the early-exercise floor on nodes < N-1 (all but
-                // the last lane's node M-1, slot P-1 .y)
-#pragma unroll
-                for (int kk = 0; kk < P; ++kk) {
-                    ff_acc2(H2[kk], L2[kk], y2[kk]);
-                    if (amer) {
-                        const float4 p = ppay[kk * NL];
-                        const float2 e = __fadd2_rn(sub2(H2[kk], make_float2(p.x, p.y)), sub2(L2[kk], make_float2(p.z, p.w)));
-                        if (e.x < 0.f) {
-                            H2[kk].x = p.x;
-                            L2[kk].x = p.z;
-                        }
-                        if (e.y < 0.f && !(kk == P - 1 && K == NL - 1)) {
-                            H2[kk].y = p.y;
-                            L2[kk].y = p.w;
-                        }
+                for (int lv = 0; lv < kLevels; ++lv) {
+                    const int sg = 1 << lv;
+                    const float rm = cur[K - sg >= 0 ? K - sg : K];
+                    const float rp = cur[K + sg < NL ? K + sg : K];
+                    rho = rho - ka[lv] * rm - kc[lv] * rp;  // ka, kc are 0 past the ends
+                    if (lv + 1 < kLevels) {
+                        nxt[K] = rho;
+                        __syncthreads();
+                        float* tmp = cur;
+                        cur = nxt;
+                        nxt = tmp;
                     }
                 }
             }
-            // ------------------------------------------------------------ result
-            double* V = vout + shape_row(sh, pde);
+            const float sv = rho * ib;
+            float s1;
+            if constexpr (W == 1) {
+                s1 = __shfl_down_sync(kFull, sv, 1);
+            } else {
+                x_s[K] = sv;
+                __syncthreads();
+                s1 = x_s[K < NL - 1 ? K + 1 : K];
+            }
+            if (K == NL - 1) s1 = 0.f;
+            const float2 ms = make_float2(-sv, -sv), ms1 = make_float2(-s1, -s1);
+#pragma unroll
+            for (int kk = 1; kk < P; ++kk) {
+                const float4 f1 = F1t[kk * kStride];
+                const float2 f2 = F2t[kk * kStride];
+                y2[kk] = __ffma2_rn(ms1, f2, __ffma2_rn(ms, make_float2(f1.z, f1.w), y2[kk]));
+            }
+            y2[0] = make_float2(sv, fmaf(-s1, fp2.y, fmaf(-sv, fp1.w, yP)));
+            // V += d (float-float), then the early-exercise floor
 #pragma unroll
             for (int kk = 0; kk < P; ++kk) {
-                V[j0 + (kk == 0 ? 0 : P - kk)] = (double)H2[kk].x + (double)L2[kk].x;
-                V[j0 + P + kk] = (double)H2[kk].y + (double)L2[kk].y;
-            }
-        } else {
-            float H[M], Lo[M];  // V as float-float pairs, starting at the payoff
-    #pragma unroll
-            for (int i = 0; i < M; ++i) {
-                const float2 p = PAY(i);
-                H[i] = p.x;
-                Lo[i] = p.y;
-            }
-
-            // ------------------------------------------------------------ time steps
-            for (int step = 1; run && step < TL; ++step) {
-                float Hm, Lm, Hp, Lp;
-                if constexpr (W == 1) {
-                    Hm = __shfl_up_sync(kFull, H[M - 1], 1);
-                    Lm = __shfl_up_sync(kFull, Lo[M - 1], 1);
-                    Hp = __shfl_down_sync(kFull, H[0], 1);
-                    Lp = __shfl_down_sync(kFull, Lo[0], 1);
-                } else {
-                    x_last[K] = make_float2(H[M - 1], Lo[M - 1]);
-                    x_first[K] = make_float2(H[0], Lo[0]);
-                    __syncthreads();
-                    const float2 pm = x_last[K > 0 ? K - 1 : 0], pp = x_first[K < NL - 1 ? K + 1 : 0];
-                    Hm = pm.x;
-                    Lm = pm.y;
-                    Hp = pp.x;
-                    Lp = pp.y;
-                }
-                if (K == 0) Hm = Lm = 0.f;
-                if (K == NL - 1) Hp = Lp = 0.f;
-                float y[M];
-                // residual r = dt A V from exact float-float differences
-    #pragma unroll
-                for (int i = 0; i < M; ++i) {
-                    const float hl = (i == 0) ? Hm : H[i - 1], ll = (i == 0) ? Lm : Lo[i - 1];
-                    const float hr = (i == M - 1) ? Hp : H[i + 1], lr = (i == M - 1) ? Lp : Lo[i + 1];
-                    const float hdu = hr - H[i], hdd = H[i] - hl, ldu = lr - Lo[i], ldd = Lo[i] - ll;
-                    const float Dup = hdu + ldu, Ddn = hdd + ldd, S = (hdu - hdd) + (ldu - ldd);
-                    if (kUni) {
-                        float r = c4u * (H[i] + Lo[i]);
-                        r = fmaf(c1u, S, r);
-                        r = fmaf(c2u, Dup, r);
-                        y[i] = fmaf(c3u, Ddn, r);
-                    } else {
-                        const float4 c = C(i);
-                        float r = c.w * (H[i] + Lo[i]);
-                        r = fmaf(c.x, S, r);
-                        r = fmaf(c.y, Dup, r);
-                        y[i] = fmaf(c.z, Ddn, r);
+                ff_acc2(H2[kk], L2[kk], y2[kk]);
+                if (amer) {
+                    const float4 p = PPt[kk * NL];
+                    const float2 e =
+                        __fadd2_rn(sub2(H2[kk], make_float2(p.x, p.y)), sub2(L2[kk], make_float2(p.z, p.w)));
+                    const bool pa = kUni || (kk == 0 ? 0 : P - kk) < lim;
+                    const bool pb = kUni ? !(kk == P - 1 && K == NL - 1) : P + kk < lim;
+                    if (e.x < 0.f && pa) {
+                        H2[kk].x = p.x;
+                        L2[kk].x = p.z;
                     }
-                }
-                if (kUni) {  // the one-sided boundary rows (no second difference)
-                    if (K == 0) y[0] = fmaf(c2b, (H[1] - H[0]) + (Lo[1] - Lo[0]), c4u * (H[0] + Lo[0]));
-                    if (K == NL - 1)
-                        y[M - 1] = fmaf(c3b, (H[M - 1] - H[M - 2]) + (Lo[M - 1] - Lo[M - 2]), c4u * (H[M - 1] + Lo[M - 1]));
-                }
-                interior_solve(y);
-                // separators: right-hand side, cyclic reduction, back to the interior
-                float ylp;
-                if constexpr (W == 1) {
-                    ylp = __shfl_up_sync(kFull, y[M - 1], 1);
-                } else {
-                    x_y[K] = y[M - 1];
-                    __syncthreads();
-                    ylp = x_y[K > 0 ? K - 1 : 0];
-                }
-                if (K == 0) ylp = 0.f;
-                float rho = y[0] - blaf * ylp - buaf * y[1];
-                if constexpr (W == 1) {
-    #pragma unroll
-                    for (int lv = 0; lv < kLevels; ++lv) {
-                        const int sg = 1 << lv;
-                        const float rm = __shfl_up_sync(kFull, rho, sg);
-                        const float rp = __shfl_down_sync(kFull, rho, sg);
-                        rho = rho - ka[lv] * rm - kc[lv] * rp;
-                    }
-                } else {
-                    float* cur = x_p0;
-                    float* nxt = x_p1;
-                    cur[K] = rho;
-                    __syncthreads();
-    #pragma unroll
-                    for (int lv = 0; lv < kLevels; ++lv) {
-                        const int sg = 1 << lv;
-                        const float rm = cur[K - sg >= 0 ? K - sg : K];
-                        const float rp = cur[K + sg < NL ? K + sg : K];
-                        rho = rho - ka[lv] * rm - kc[lv] * rp;  // ka, kc are 0 past the ends
-                        if (lv + 1 < kLevels) {
-                            nxt[K] = rho;
-                            __syncthreads();
-                            float* tmp = cur;
-                            cur = nxt;
-                            nxt = tmp;
-                        }
-                    }
-                }
-                const float s = rho * ib;
-                float s1;
-                if constexpr (W == 1) {
-                    s1 = __shfl_down_sync(kFull, s, 1);
-                } else {
-                    x_s[K] = s;
-                    __syncthreads();
-                    s1 = x_s[K < NL - 1 ? K + 1 : K];
-                }
-                if (K == NL - 1) s1 = 0.f;
-                y[0] = s;
-    #pragma unroll
-                for (int i = 1; i < M; ++i) {
-                    const float2 sp = SPK(i);
-                    y[i] = fmaf(-s1, sp.y, fmaf(-s, sp.x, y[i]));
-                }
-                // V += d (float-float), then the early-exercise floor on nodes < N-1
-    #pragma unroll
-                for (int i = 0; i < M; ++i) {
-                    ff_acc(H[i], Lo[i], y[i]);
-                    if (amer && j0 + i < N - 1) {
-                        const float2 p = PAY(i);
-                        if ((H[i] - p.x) + (Lo[i] - p.y) < 0.f) {
-                            H[i] = p.x;
-                            Lo[i] = p.y;
-                        }
+                    if (e.y < 0.f && pb) {
+                        H2[kk].y = p.y;
+                        L2[kk].y = p.w;
                     }
                 }
             }
-            // ------------------------------------------------------------ result
-            double* V = vout + shape_row(sh, pde);
-    #pragma unroll
-            for (int i = 0; i < M; ++i)
-                if (j0 + i < N) V[j0 + i] = (double)H[i] + (double)Lo[i];
+        }
+        // ------------------------------------------------------------ result
+        double* V = vout + shape_row(sh, pde);
+#pragma unroll
+        for (int kk = 0; kk < P; ++kk) {
+            const int na = j0 + (kk == 0 ? 0 : P - kk), nb = j0 + P + kk;
+            if (na < N) V[na] = (double)H2[kk].x + (double)L2[kk].x;
+            if (nb < N) V[nb] = (double)H2[kk].y + (double)L2[kk].y;
         }
         if (K == 0) pde_status[pde] = st;
     }
@@ -802,8 +770,7 @@ int& per_sm_fp32()
 template <int M, bool kUni, int W>
 constexpr size_t fp32_smem()
 {
-    return ((size_t)M * f32_fields<kUni>() * 32 * W + (kUni ? (size_t)M * kSharedFields * 2 : 0) +
-            (size_t)f32_pair_floats<M, kUni, W>()) * sizeof(float) +
+    return ((size_t)M * f32_fields<kUni>() * 32 * W + (kUni ? (size_t)M * kSharedFields * 2 : 0)) * sizeof(float) +
            f32_xchg_bytes<W>();
 }
 
