@@ -129,24 +129,18 @@ constexpr double kFreeze = 0x1p-50;
 
 }  // namespace
 
-// One thread per PDE slot.  Builds the grid, payoff and both factorisations of
-// theta*B, writes CU, CD, P, S (V = payoff), the middle-region constants, and runs
-// the first (DOWN) elimination on V so that the solve starts with an UP sweep.
-__global__ void __launch_bounds__(128) fd1d_setup_fp64(const PdeBatch b, Fd1dShape sh, double* __restrict__ base,
-                                                       int32_t* __restrict__ pde_status)
+namespace {
+
+// The setup of one PDE slot.  cw, cl: the width of the tile's coefficient and payoff
+// records and this slot's index in them -- kTile and the lane, or in twin tiles 16 and
+// lane / 2 (one record per twin pair).
+__device__ __forceinline__ void setup_slot(const PdeBatch& b, const Fd1dShape& sh, const Work& wk, const TileView& tv,
+                                           int slot, int src, int lane, int N, int cw, int cl,
+                                           int32_t* __restrict__ pde_status)
 {
-    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= b.m_pad) return;
-    const int src = slot < b.m ? slot : b.m - 1;  // padding lanes replicate the last PDE
-    const int tile = slot / kTile, lane = slot % kTile;
-    int N;
-    long long toff;
-    tile_shape(sh, tile, N, toff);
-    const Work wk = work_of(base, b.m_pad, sh.node_lanes);
-    const TileView tv = tile_view(wk, toff);
-    auto CU = [&](int j, int f) -> double& { return tv.cu[((size_t)j * kCoef + f) * kTile + lane]; };
-    auto CD = [&](int j, int f) -> double& { return tv.cd[((size_t)j * kCoef + f) * kTile + lane]; };
-    auto P = [&](int j) -> double& { return tv.p[(size_t)j * kTile + lane]; };
+    auto CU = [&](int j, int f) -> double& { return tv.cu[((size_t)j * kCoef + f) * cw + cl]; };
+    auto CD = [&](int j, int f) -> double& { return tv.cd[((size_t)j * kCoef + f) * cw + cl]; };
+    auto P = [&](int j) -> double& { return tv.p[(size_t)j * cw + cl]; };
     auto S = [&](int j, int f) -> double& { return tv.s[((size_t)j * kTile + lane) * 2 + f]; };
 
     const double t = b.t[src], z = b.z[src];
@@ -274,6 +268,42 @@ __global__ void __launch_bounds__(128) fd1d_setup_fp64(const PdeBatch b, Fd1dSha
     if (slot < b.m) pde_status[slot] = st;
 }
 
+}  // namespace
+
+// One thread per PDE slot.  Builds the grid, payoff and both factorisations of
+// theta*B, writes CU, CD, P, S (V = payoff), the middle-region constants, and runs
+// the first (DOWN) elimination on V so that the solve starts with an UP sweep.
+__global__ void __launch_bounds__(128) fd1d_setup_fp64(const PdeBatch b, Fd1dShape sh, double* __restrict__ base,
+                                                       int32_t* __restrict__ pde_status)
+{
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= b.m_pad) return;  // whole warps: m_pad is a multiple of the tile
+    const int src = slot < b.m ? slot : b.m - 1;  // padding lanes replicate the last PDE
+    const int tile = slot / kTile, lane = slot % kTile;
+    int N;
+    long long toff;
+    tile_shape(sh, tile, N, toff);
+    const Work wk = work_of(base, b.m_pad, sh.node_lanes);
+    const TileView tv = tile_view(wk, toff);
+    const bool twin = tile < sh.twin_tiles;
+    // in a twin tile the odd lane (the European copy) has the same operator, payoff and
+    // first elimination as the American PDE before it: it copies them below
+    const bool copy = twin && (lane & 1);
+    if (!copy) setup_slot(b, sh, wk, tv, slot, src, lane, N, twin ? kTile / 2 : kTile, twin ? lane >> 1 : lane,
+                          pde_status);
+    if (twin) {
+        __syncwarp();
+        if (copy) {
+            double2* sv = reinterpret_cast<double2*>(tv.s);
+            for (int j = 0; j < N; ++j) sv[(size_t)j * kTile + lane] = sv[(size_t)j * kTile + lane - 1];
+            for (int c = 0; c < kConsts; ++c) wk.cst[(size_t)slot * kConsts + c] = wk.cst[(size_t)(slot - 1) * kConsts + c];
+            wk.range[slot] = wk.range[slot - 1];
+            wk.zero[slot] = make_int2(0, N - 1);  // European: never projects
+            if (slot < b.m) pde_status[slot] = pde_status[slot - 1];
+        }
+    }
+}
+
 namespace {
 
 // Ring of stage slots in shared memory; a slot holds kGroup consecutive nodes of one
@@ -377,31 +407,38 @@ __device__ __forceinline__ int stage_after(int cur, const Stage& s)
     return kUp ? cur + s.count : cur - s.count;
 }
 
+// Twin tiles hold one coefficient and payoff record per twin pair: 16 entries per node
+// where other tiles hold 32.
+template <bool kTwin>
+__host__ __device__ constexpr int rec_width() { return kTwin ? kTile / 2 : kTile; }
+
 // Bytes a stage moves: its bulk reads plus the state stores.
-__device__ __forceinline__ unsigned long long stage_bytes(const Stage& s)
+__device__ __forceinline__ unsigned long long stage_bytes(const Stage& s, bool twin)
 {
-    return (unsigned long long)s.count * (2 * kNodeSBytes + (s.pfree ? 0 : kNodePBytes) +
-                                          (s.compact ? 0 : kNodeCoefBytes));
+    const unsigned long long rec = (s.pfree ? 0 : kNodePBytes) + (s.compact ? 0 : kNodeCoefBytes);
+    return (unsigned long long)s.count * (2 * kNodeSBytes + (twin ? rec / 2 : rec));
 }
 
-// Issues stage visit q for stage sg of this tile.
-template <bool kUp>
+// Issues stage visit q for stage sg of this tile.  Twin tiles copy half-width
+// coefficient and payoff records into the front of the same slot areas.
+template <bool kUp, bool kTwin>
 __device__ __forceinline__ void issue(const Ring& r, uint32_t q, const TileView& tv, const Stage& sg, uint64_t pol)
 {
+    constexpr int kW = rec_width<kTwin>();
     const int s = (int)(q % kRing);
     unsigned char* st = r.stage + (size_t)s * kStageBytes;
-    const uint32_t cb = sg.compact ? 0u : sg.count * kNodeCoefBytes;
-    const uint32_t pb = sg.pfree ? 0u : sg.count * kNodePBytes, sb = sg.count * kNodeSBytes;
+    const uint32_t cb = sg.compact ? 0u : sg.count * (uint32_t)(kCoef * kW * 8);
+    const uint32_t pb = sg.pfree ? 0u : sg.count * (uint32_t)(kW * 8), sb = sg.count * kNodeSBytes;
     const uint32_t p_off = sg.wide ? 0u : kStageCoef, s_off = sg.wide ? kWideP : kStageCoef + kStageP;
     mbar_arrive_expect_tx(&r.bar[s], cb + pb + sb);
-    if (cb) bulk_g2s_hint(st, (kUp ? tv.cu : tv.cd) + (size_t)sg.first * kCoef * kTile, cb, &r.bar[s], pol);
-    if (pb) bulk_g2s_hint(st + p_off, tv.p + (size_t)sg.first * kTile, pb, &r.bar[s], pol);
+    if (cb) bulk_g2s_hint(st, (kUp ? tv.cu : tv.cd) + (size_t)sg.first * kCoef * kW, cb, &r.bar[s], pol);
+    if (pb) bulk_g2s_hint(st + p_off, tv.p + (size_t)sg.first * kW, pb, &r.bar[s], pol);
     bulk_g2s_hint(st + s_off, tv.s + (size_t)sg.first * kTile * 2, sb, &r.bar[s], pol);
 }
 
 // The refilling side of a sweep, run by lane 0: the next stage to issue and its
 // visit number.
-template <bool kUp>
+template <bool kUp, bool kTwin>
 struct Producer {
     int cur;
     uint32_t next;
@@ -409,7 +446,7 @@ struct Producer {
     {
         if (sweep_done<kUp>(cur, N)) return;
         const Stage sg = stage_at<kUp>(cur, N, rg);
-        issue<kUp>(ring, next, tv, sg, pol);
+        issue<kUp, kTwin>(ring, next, tv, sg, pol);
         cur = stage_after<kUp>(cur, sg);
         ++next;
     }
@@ -448,26 +485,28 @@ __device__ __forceinline__ void stage_steps(const double* ra, const double* rb, 
 // and runs its node-steps.  kCompact: the stage lies in the middle region
 // (coefficients ca, cb, cs).  No per-node guard: the unrolled stage is one block the
 // scheduler interleaves across nodes.
-template <bool kUp, bool kHalf, bool kCompact>
-__device__ __forceinline__ void stage_body(const Ring& ring, const TileView& tv, Producer<kUp>& prod, int N,
+template <bool kUp, bool kHalf, bool kCompact, bool kTwin>
+__device__ __forceinline__ void stage_body(const Ring& ring, const TileView& tv, Producer<kUp, kTwin>& prod, int N,
                                            const Ranges& rg, int first, bool pfree, const unsigned char* st, int lane,
                                            double ca, double cb, double cs, double c, bool amer, bool active,
                                            double2* sout, const Hints& hz, double& yh, double& f)
 {
-    const double* sc_ = reinterpret_cast<const double*>(st) + lane;
-    const double* sp_ = reinterpret_cast<const double*>(st + kStageCoef) + lane;
+    constexpr int kW = rec_width<kTwin>();
+    const int rl = kTwin ? lane >> 1 : lane;  // this lane's entry of the records
+    const double* sc_ = reinterpret_cast<const double*>(st) + rl;
+    const double* sp_ = reinterpret_cast<const double*>(st + kStageCoef) + rl;
     const double2* ss_ = reinterpret_cast<const double2*>(st + kStageCoef + kStageP) + lane;
     double ra[kGroup], rb[kGroup], rs[kGroup], rp[kGroup], rv[kGroup], rw[kGroup];
 #pragma unroll
     for (int k = 0; k < kGroup; ++k) {
         const int idx = kUp ? k : kGroup - 1 - k;  // processing order within the stage
-        rp[k] = pfree ? 0. : sp_[idx * kTile];
+        rp[k] = pfree ? 0. : sp_[idx * kW];
         const double2 sv = ss_[idx * kTile];
         rv[k] = sv.x;
         rw[k] = sv.y;
-        ra[k] = kCompact ? ca : sc_[(idx * kCoef + 0) * kTile];
-        rb[k] = kCompact ? cb : sc_[(idx * kCoef + 1) * kTile];
-        rs[k] = kCompact ? cs : sc_[(idx * kCoef + 2) * kTile];
+        ra[k] = kCompact ? ca : sc_[(idx * kCoef + 0) * kW];
+        rb[k] = kCompact ? cb : sc_[(idx * kCoef + 1) * kW];
+        rs[k] = kCompact ? cs : sc_[(idx * kCoef + 2) * kW];
     }
     __syncwarp();  // the slot fully read before it is refilled
     if (lane == 0) prod.refill(ring, tv, N, rg, hz.stream);
@@ -475,19 +514,21 @@ __device__ __forceinline__ void stage_body(const Ring& ring, const TileView& tv,
 }
 
 // One wide stage (kWide middle-region nodes, wide layout).
-template <bool kUp, bool kHalf>
-__device__ __forceinline__ void stage_body_wide(const Ring& ring, const TileView& tv, Producer<kUp>& prod, int N,
-                                                const Ranges& rg, int first, bool pfree, const unsigned char* st,
-                                                int lane, double ca, double cb, double cs, double c, bool amer,
-                                                bool active, double2* sout, const Hints& hz, double& yh, double& f)
+template <bool kUp, bool kHalf, bool kTwin>
+__device__ __forceinline__ void stage_body_wide(const Ring& ring, const TileView& tv, Producer<kUp, kTwin>& prod,
+                                                int N, const Ranges& rg, int first, bool pfree,
+                                                const unsigned char* st, int lane, double ca, double cb, double cs,
+                                                double c, bool amer, bool active, double2* sout, const Hints& hz,
+                                                double& yh, double& f)
 {
-    const double* sp_ = reinterpret_cast<const double*>(st) + lane;
+    constexpr int kW = rec_width<kTwin>();
+    const double* sp_ = reinterpret_cast<const double*>(st) + (kTwin ? lane >> 1 : lane);
     const double2* ss_ = reinterpret_cast<const double2*>(st + kWideP) + lane;
     double ra[kWide], rb[kWide], rs[kWide], rp[kWide], rv[kWide], rw[kWide];
 #pragma unroll
     for (int k = 0; k < kWide; ++k) {
         const int idx = kUp ? k : kWide - 1 - k;
-        rp[k] = pfree ? 0. : sp_[idx * kTile];
+        rp[k] = pfree ? 0. : sp_[idx * kW];
         const double2 sv = ss_[idx * kTile];
         rv[k] = sv.x;
         rw[k] = sv.y;
@@ -503,26 +544,28 @@ __device__ __forceinline__ void stage_body_wide(const Ring& ring, const TileView
 // A sweep's last stage when it holds fewer than kGroup nodes.  It refills no ring
 // slot (no later stage), so it reads shared memory node by node in a rolled loop
 // and holds no stage in registers.
-template <bool kUp, bool kHalf>
+template <bool kUp, bool kHalf, bool kTwin>
 __device__ __forceinline__ void tail_stage(int first, int count, bool compact, bool pfree, const unsigned char* st,
                                            int lane, double ca, double cb, double cs, double c, bool amer,
                                            bool active, int N, double2* sout, const Hints& hz, double& yh,
                                            double& f)
 {
-    const double* sc_ = reinterpret_cast<const double*>(st) + lane;
-    const double* sp_ = reinterpret_cast<const double*>(st + kStageCoef) + lane;
+    constexpr int kW = rec_width<kTwin>();
+    const int rl = kTwin ? lane >> 1 : lane;
+    const double* sc_ = reinterpret_cast<const double*>(st) + rl;
+    const double* sp_ = reinterpret_cast<const double*>(st + kStageCoef) + rl;
     const double2* ss_ = reinterpret_cast<const double2*>(st + kStageCoef + kStageP) + lane;
 #pragma unroll 1
     for (int k = 0; k < count; ++k) {
         const int idx = kUp ? k : count - 1 - k;
         const int j = first + idx;
         const double2 sv = ss_[idx * kTile];
-        const double a = compact ? ca : sc_[(idx * kCoef + 0) * kTile];
-        const double bb = compact ? cb : sc_[(idx * kCoef + 1) * kTile];
-        const double sg = compact ? cs : sc_[(idx * kCoef + 2) * kTile];
+        const double a = compact ? ca : sc_[(idx * kCoef + 0) * kW];
+        const double bb = compact ? cb : sc_[(idx * kCoef + 1) * kW];
+        const double sg = compact ? cs : sc_[(idx * kCoef + 2) * kW];
         yh = fma(-a, yh, sv.y);
         double vn = kHalf ? fma(sg, yh, -sv.x) : fma(sg, yh, -c * sv.x);
-        if (amer && j < N - 1) vn = max_floor(vn, pfree ? 0. : sp_[idx * kTile]);
+        if (amer && j < N - 1) vn = max_floor(vn, pfree ? 0. : sp_[idx * kW]);
         f = fma(-bb, f, vn);
         if (active)
             st_global_f64x2_hint(reinterpret_cast<double*>(sout + (size_t)j * kTile), vn, f,
@@ -532,7 +575,7 @@ __device__ __forceinline__ void tail_stage(int first, int count, bool compact, b
 
 // One sweep over this warp's tile.  Returns the stage visits it consumed, or -1 on a
 // wait timeout (copies in flight already drained).
-template <bool kUp, bool kHalf>
+template <bool kUp, bool kHalf, bool kTwin>
 __device__ __forceinline__ int sweep(const Ring& ring, uint32_t q, const TileView& tv, int lane, int N,
                                      const Ranges& rg, const double* cst, double c, bool amer, bool active,
                                      const Hints& hz, int* err)
@@ -540,7 +583,7 @@ __device__ __forceinline__ int sweep(const Ring& ring, uint32_t q, const TileVie
     // the previous sweep's stores must be visible to the bulk-copy engine
     fence_proxy_async_global();
     __syncwarp();
-    Producer<kUp> prod{sweep_first<kUp>(N), q};
+    Producer<kUp, kTwin> prod{sweep_first<kUp>(N), q};
     if (lane == 0)
         for (int i = 0; i < kRing; ++i) prod.refill(ring, tv, N, rg, hz.stream);
     // middle-region constants: UP uses (nh, l, 1/e), DOWN (uh, m, 1/d)
@@ -562,17 +605,17 @@ __device__ __forceinline__ int sweep(const Ring& ring, uint32_t q, const TileVie
         const Stage sg = stage_at<kUp>(cur, N, rg);
         const unsigned char* st = ring.stage + (size_t)s * kStageBytes;
         if (sg.wide)
-            stage_body_wide<kUp, kHalf>(ring, tv, prod, N, rg, sg.first, sg.pfree, st, lane, ca, cb, cs, c, amer,
-                                        active, sout, hz, yh, f);
+            stage_body_wide<kUp, kHalf, kTwin>(ring, tv, prod, N, rg, sg.first, sg.pfree, st, lane, ca, cb, cs, c,
+                                               amer, active, sout, hz, yh, f);
         else if (sg.count == kGroup && sg.compact)
-            stage_body<kUp, kHalf, true>(ring, tv, prod, N, rg, sg.first, sg.pfree, st, lane, ca, cb, cs, c, amer,
-                                         active, sout, hz, yh, f);
+            stage_body<kUp, kHalf, true, kTwin>(ring, tv, prod, N, rg, sg.first, sg.pfree, st, lane, ca, cb, cs, c,
+                                                amer, active, sout, hz, yh, f);
         else if (sg.count == kGroup)
-            stage_body<kUp, kHalf, false>(ring, tv, prod, N, rg, sg.first, sg.pfree, st, lane, ca, cb, cs, c, amer,
-                                          active, sout, hz, yh, f);
+            stage_body<kUp, kHalf, false, kTwin>(ring, tv, prod, N, rg, sg.first, sg.pfree, st, lane, ca, cb, cs, c,
+                                                 amer, active, sout, hz, yh, f);
         else
-            tail_stage<kUp, kHalf>(sg.first, sg.count, sg.compact, sg.pfree, st, lane, ca, cb, cs, c, amer, active,
-                                   N, sout, hz, yh, f);
+            tail_stage<kUp, kHalf, kTwin>(sg.first, sg.count, sg.compact, sg.pfree, st, lane, ca, cb, cs, c, amer,
+                                          active, N, sout, hz, yh, f);
         cur = stage_after<kUp>(cur, sg);
     }
     return (int)(v - q);
@@ -626,6 +669,7 @@ __global__ void __launch_bounds__(32 * kMaxBlockWarps)
         long long toff;
         tile_shape(sh, tile, N, toff);
         const TileView tv = tile_view(wk, toff);
+        const bool twin = tile < sh.twin_tiles;  // one coefficient and payoff record per lane pair
         // every lane steps its own PDE tDim-1 times; the tile runs for its longest
         const int t_lane = shape_t(sh, src);
         const int t_max = sh.tiles ? sh.tiles[tile].t_max : sh.t_dim;
@@ -645,12 +689,12 @@ __global__ void __launch_bounds__(32 * kMaxBlockWarps)
             unsigned long long per_up = 0, per_dn = 0;
             for (int cur = sweep_first<true>(N); !sweep_done<true>(cur, N);) {
                 const Stage sg = stage_at<true>(cur, N, rg);
-                per_up += stage_bytes(sg);
+                per_up += stage_bytes(sg, twin);
                 cur = stage_after<true>(cur, sg);
             }
             for (int cur = sweep_first<false>(N); !sweep_done<false>(cur, N);) {
                 const Stage sg = stage_at<false>(cur, N, rg);
-                per_dn += stage_bytes(sg);
+                per_dn += stage_bytes(sg, twin);
                 cur = stage_after<false>(cur, sg);
             }
             const unsigned long long n_up = (unsigned long long)(t_max / 2);  // passes 1, 3, 5, ...
@@ -661,10 +705,17 @@ __global__ void __launch_bounds__(32 * kMaxBlockWarps)
         ht.keep_n = min(hz.keep_n, N / 2);
         for (int pass = 1; pass < t_max; ++pass) {
             const bool act = pass < t_lane;
-            const int used = (pass & 1) ? sweep<true, kHalf>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act, ht,
+            int used;
+            if (twin)
+                used = (pass & 1) ? sweep<true, kHalf, true>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act, ht,
                                                              &tile_counter[1])
-                                        : sweep<false, kHalf>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act, ht,
+                                  : sweep<false, kHalf, true>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act, ht,
                                                               &tile_counter[1]);
+            else
+                used = (pass & 1) ? sweep<true, kHalf, false>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act, ht,
+                                                              &tile_counter[1])
+                                  : sweep<false, kHalf, false>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act, ht,
+                                                               &tile_counter[1]);
             if (used < 0) return;
             q += (uint32_t)used;
         }

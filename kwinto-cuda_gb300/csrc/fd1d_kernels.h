@@ -64,6 +64,10 @@ struct Fd1dShape {
     int option_warps = 1;
     int sm_blocks = 0;  // FP64 streaming solver: resident blocks per SM (0: as many as fit)
     int keep_nodes = 0;  // FP64 streaming solver: nodes at each sweep's end stored evict-last in L2 (set by the launch)
+    // FP64 streaming solver, uniform batches: tiles [0, twin_tiles) hold 16 twin pairs
+    // each -- an American PDE in the even lane, its European copy (same t, r, q, z, w)
+    // in the odd lane -- which read one shared record of coefficients and payoff
+    int twin_tiles = 0;
 };
 
 __host__ __device__ inline int shape_x(const Fd1dShape& sh, int pde) { return sh.pde_x ? sh.pde_x[pde] : sh.x_dim; }

@@ -16,6 +16,7 @@
 #include <numeric>
 #include <string>
 #include <tuple>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -265,7 +266,7 @@ kwg_ctx::Tuned choose(kwg_ctx* ctx, const kwg_fd1d_params* p, int m)
 }
 
 int run_batch(kwg_ctx* ctx, char* io, const IoLayout& L, int m, int n, const kwg_fd1d_params* p,
-              double* prices, int32_t* status, cudaStream_t stream)
+              double* prices, int32_t* status, cudaStream_t stream, int twin_tiles = 0)
 {
     const int m_pad = (m + kwg::kTile - 1) / kwg::kTile * kwg::kTile;
     kwg::PdeBatch b;
@@ -283,6 +284,7 @@ int run_batch(kwg_ctx* ctx, char* io, const IoLayout& L, int m, int n, const kwg
     a.pde = (const int32_t*)(io + L.pde);
     a.n = n;
     kwg::Fd1dShape sh = make_shape(p);
+    sh.twin_tiles = twin_tiles;
     const kwg_ctx::Tuned tn = choose(ctx, p, m);
     const int solver = tn.solver;
     sh.block_warps = tn.block_warps;
@@ -349,14 +351,41 @@ int price_host(kwg_ctx* ctx, const kwg_option* user_opts, size_t n_user, const k
     std::vector<uint32_t> pde2asset;
     const size_t m = kwg::dedup_host(opts, n, nullptr, nullptr, asset2pde, pde2asset);
     const size_t m_pad = (m + kwg::kTile - 1) / kwg::kTile * kwg::kTile;
-    // PDEs grouped by exercise / put-call class (stable), so tiles are homogeneous
+    // PDE order.  FD1D-BS: each American PDE and its European copy (the PDE of the
+    // asset's European twin, same t, r, q, z, w) go to lanes 2k, 2k+1 of the first
+    // tiles -- puts first, then calls -- as many whole tiles of 16 pairs as there are;
+    // the streaming FP64 solver then reads one coefficient and payoff record per pair.
+    // All other PDEs follow grouped by exercise / put-call class (stable), so tiles are
+    // homogeneous.
+    int twin_tiles = 0;
     {
-        size_t off[5] = {0, 0, 0, 0, 0};
-        for (uint32_t a : pde2asset) ++off[pde_class(opts[a].e, opts[a].w) + 1];
-        for (int c = 0; c < 4; ++c) off[c + 1] += off[c];
-        std::vector<int32_t> moved(m);
+        std::vector<int32_t> moved(m, -1);
         std::vector<uint32_t> order2(m);
+        size_t placed = 0;
+        if (control_variate) {
+            std::vector<std::pair<uint32_t, uint32_t>> pairs;
+            for (int put_first = 1; put_first >= 0; --put_first)
+                for (size_t j = 0; j < m; ++j) {
+                    const uint32_t a = pde2asset[j];
+                    if (a >= n_user || !opts[a].e || (opts[a].w < 0) != (put_first == 1)) continue;
+                    const uint32_t je = (uint32_t)asset2pde[n_user + a];
+                    if (je != j) pairs.emplace_back((uint32_t)j, je);
+                }
+            twin_tiles = (int)(pairs.size() / (kwg::kTile / 2));
+            for (size_t k = 0; k < (size_t)twin_tiles * (kwg::kTile / 2); ++k) {
+                for (const uint32_t j : {pairs[k].first, pairs[k].second}) {
+                    moved[j] = (int32_t)placed;
+                    order2[placed++] = pde2asset[j];
+                }
+            }
+        }
+        size_t off[5] = {0, 0, 0, 0, 0};
+        for (size_t j = 0; j < m; ++j)
+            if (moved[j] < 0) ++off[pde_class(opts[pde2asset[j]].e, opts[pde2asset[j]].w) + 1];
+        off[0] = placed;
+        for (int c = 0; c < 4; ++c) off[c + 1] += off[c];
         for (size_t j = 0; j < m; ++j) {
+            if (moved[j] >= 0) continue;
             const uint32_t a = pde2asset[j];
             const size_t to = off[pde_class(opts[a].e, opts[a].w)]++;
             moved[j] = (int32_t)to;
@@ -395,7 +424,7 @@ int price_host(kwg_ctx* ctx, const kwg_option* user_opts, size_t n_user, const k
     // 3. kernels
     char* dio = (char*)ctx->d_io;
     if (int rc = run_batch(ctx, dio, L, (int)m, (int)n, p, (double*)(dio + L.prices), (int32_t*)(dio + L.status),
-                           ctx->stream))
+                           ctx->stream, twin_tiles))
         return rc;
     if (control_variate) {
         bs_control_variate<<<(unsigned)((n_user + 255) / 256), 256, 0, ctx->stream>>>(

@@ -119,3 +119,36 @@ def test_pricer_factory(ctx):
     prices = [0.0] * len(g["opts"])
     assert pricer.price(g["opts"], prices) == ""
     assert rel_err(np.array(prices), g["ref_fd1d_bs"]) <= REL_TOL
+
+
+@pytest.mark.parametrize("density", [0.25, math.inf])
+def test_twin_tiles_streaming_solver(ctx, density):
+    """The streaming FP64 solver runs each American PDE beside its European copy
+    (lanes 2k, 2k+1 of the first tiles) on one shared coefficient and payoff record.
+    A mix of American and European puts and calls with duplicates: 2 x 16 x 21 twin
+    pairs fill 21 twin tiles with leftovers in ordinary tiles, against the oracle."""
+    import kwor
+    import portfolio
+
+    o = portfolio.american_portfolio(700, seed=41)
+    o["w"][::2] = -o["w"][::2]
+    o["e"][5::7] = 0
+    o = np.concatenate([o, o[:60]])  # duplicates share their PDEs
+    kw = dict(t_dim=257, x_dim=384, scale=5.0, density=density)
+    p, st = bs_price(ctx, o, solver=1, **kw)
+    rc, msg, want, _ = kwor.fd1d_price(o, bs=True, **kw)
+    assert rc == 0, msg
+    assert (st == 0).all()
+    assert rel_err(p, want) <= REL_TOL
+
+
+def test_twin_tiles_qdfp_portfolio(ctx):
+    """6000 American puts at the reference defaults through the streaming solver:
+    600 twin pairs, 37 twin tiles."""
+    import kwor
+
+    g = golden("portfolio_qdfp.npz")
+    p, st = bs_price(ctx, g["opts"], solver=1)
+    rc, msg, want, _ = kwor.fd1d_price(g["opts"], bs=True, nthreads=16)
+    assert rc == 0, msg
+    assert (st == 0).all() and rel_err(p, want) <= REL_TOL
