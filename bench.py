@@ -500,28 +500,37 @@ def run_ours(args):
     err32 = np.abs(p32 - gpu_prices)
 
     # ---------------------------------------------------------------- FD1D-BS control variate (host API)
-    for _ in range(max(1, args.warmup)):
-        rc, pbs, stbs = ctx.fd1d_bs_price(opts, prm)
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        rc, pbs, stbs = ctx.fd1d_bs_price(opts, prm)
-        if rc != 0:
-            raise RuntimeError(ctx.last_error())
-    dtbs = max_over_ranks(time.perf_counter() - t0) / args.steps
-    fd1d_bs = {"options_per_sec_e2e": n_job / dtbs, "ms_per_batch_e2e": dtbs * 1e3,
+    # on the benchmark's uniform grid and on the reference's default sinh grid
+    # (density 0.25), where the coefficients stream at every node and the American and
+    # European PDEs of an option share one record (twin tiles)
+    fd1d_bs = {}
+    for bs_name, bs_density in (("uniform", DENSITY), ("sinh_density_0.25", 0.25)):
+        prm_bs = kwg.params(t_dim=T_DIM, x_dim=X_DIM, scale=SCALE, density=bs_density, precision=kwg.FP64)
+        for _ in range(max(1, args.warmup)):
+            rc, pbs, stbs = ctx.fd1d_bs_price(opts, prm_bs)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            rc, pbs, stbs = ctx.fd1d_bs_price(opts, prm_bs)
+            if rc != 0:
+                raise RuntimeError(ctx.last_error())
+        dtbs = max_over_ranks(time.perf_counter() - t0) / args.steps
+        leg = {"options_per_sec_e2e": n_job / dtbs, "ms_per_batch_e2e": dtbs * 1e3, "density": bs_density,
                "pdes_solved": 2 * n_loc, "launches": ctx.launch_count()}
-    if not args.no_cpu and rank == 0:
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        import kwor
+        if not args.no_cpu and rank == 0:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import kwor
 
-        idx = np.arange(0, n_loc, max(1, n_loc // 512))
-        rcb, msgb, wantbs, _ = kwor.fd1d_price(opts[idx], bs=True, t_dim=T_DIM, x_dim=X_DIM, scale=SCALE,
-                                               density=DENSITY)
-        if rcb != 0:
-            raise RuntimeError(msgb)
-        fd1d_bs["max_rel_err_vs_oracle"] = float(np.max(np.abs(pbs[idx] - wantbs) / np.abs(wantbs)))
-        fd1d_bs["oracle_sample"] = len(idx)
+            idx = np.arange(0, n_loc, max(1, n_loc // 512))
+            rcb, msgb, wantbs, _ = kwor.fd1d_price(opts[idx], bs=True, t_dim=T_DIM, x_dim=X_DIM, scale=SCALE,
+                                                   density=bs_density)
+            if rcb != 0:
+                raise RuntimeError(msgb)
+            # a deep out-of-the-money control-variate price is a cancellation residue:
+            # below 1e-3 the error is taken absolutely (relative to 1e-3)
+            leg["max_rel_err_vs_oracle"] = float(np.max(np.abs(pbs[idx] - wantbs) / np.maximum(np.abs(wantbs), 1e-3)))
+            leg["oracle_sample"] = len(idx)
+        fd1d_bs[bs_name] = leg
 
     # ---------------------------------------------------------------- uneven batch (131072 options, per-option grids)
     uneven = {}
