@@ -463,22 +463,38 @@ __device__ void drain(const Ring& r, uint32_t from, uint32_t to)
 // elimination recurrence yh, the new value with the early-exercise floor, the
 // second recurrence f, and the 16-byte (value, f) store of each node.
 template <bool kUp, bool kHalf, int kG>
-__device__ __forceinline__ void stage_steps(const double* ra, const double* rb, const double* rs, const double* rp,
-                                            const double* rv, const double* rw, int first, int N, double c,
-                                            bool amer, bool active, double2* sout, const Hints& hz, double& yh,
-                                            double& f)
+__device__ __forceinline__ void stage_steps(const double* ra, const double* rb, const double* rs, const long long* rp,
+                                            const double* rv, const double* rw, int first, double c, bool active,
+                                            double2* sout, uint64_t pol, double& yh, double& f)
 {
 #pragma unroll
     for (int k = 0; k < kG; ++k) {
         const int j = kUp ? first + k : first + kG - 1 - k;
         yh = fma(-ra[k], yh, rw[k]);
-        double vn = kHalf ? fma(rs[k], yh, -rv[k]) : fma(rs[k], yh, -c * rv[k]);
-        if (amer && j < N - 1) vn = max_floor(vn, rp[k]);
+        const double vs = kHalf ? fma(rs[k], yh, -rv[k]) : fma(rs[k], yh, -c * rv[k]);
+        // the early-exercise floor as one signed 64-bit max (rp: the payoff's bits, or
+        // those of -0 where the floor does not apply, which no value falls below)
+        const double vn = __longlong_as_double(max(__double_as_longlong(vs), rp[k]));
         f = fma(-rb[k], f, vn);
-        if (active)
-            st_global_f64x2_hint(reinterpret_cast<double*>(sout + (size_t)j * kTile), vn, f,
-                                 (kUp ? j >= N - hz.keep_n : j < hz.keep_n) ? hz.keep : hz.stream);
+        if (active) st_global_f64x2_hint(reinterpret_cast<double*>(sout + (size_t)j * kTile), vn, f, pol);
     }
+}
+
+// The floor operand of node j: the payoff's bits where the reference projects
+// (American PDEs, nodes 0 .. N-2), else those of -0 (the smallest signed 64-bit
+// pattern a double has), so that the max leaves the value unchanged.
+__device__ __forceinline__ long long floor_bits(double p, bool amer, int j, int N)
+{
+    return (amer && j < N - 1) ? __double_as_longlong(p) : (long long)0x8000000000000000ull;
+}
+
+// The L2 policy of a stage's state stores: evict-last when the stage reaches into the
+// sweep's last keep_n nodes (read back first by the next sweep), evict-first otherwise.
+template <bool kUp>
+__device__ __forceinline__ uint64_t stage_policy(int first, int count, int N, const Hints& hz)
+{
+    const bool keep = kUp ? first + count - 1 >= N - hz.keep_n : first < hz.keep_n;
+    return keep ? hz.keep : hz.stream;
 }
 
 // One full kGroup-node stage: loads it into registers, lets lane 0 refill the slot,
@@ -496,11 +512,12 @@ __device__ __forceinline__ void stage_body(const Ring& ring, const TileView& tv,
     const double* sc_ = reinterpret_cast<const double*>(st) + rl;
     const double* sp_ = reinterpret_cast<const double*>(st + kStageCoef) + rl;
     const double2* ss_ = reinterpret_cast<const double2*>(st + kStageCoef + kStageP) + lane;
-    double ra[kGroup], rb[kGroup], rs[kGroup], rp[kGroup], rv[kGroup], rw[kGroup];
+    double ra[kGroup], rb[kGroup], rs[kGroup], rv[kGroup], rw[kGroup];
+    long long rp[kGroup];
 #pragma unroll
     for (int k = 0; k < kGroup; ++k) {
         const int idx = kUp ? k : kGroup - 1 - k;  // processing order within the stage
-        rp[k] = pfree ? 0. : sp_[idx * kW];
+        rp[k] = floor_bits(pfree ? 0. : sp_[idx * kW], amer, first + idx, N);
         const double2 sv = ss_[idx * kTile];
         rv[k] = sv.x;
         rw[k] = sv.y;
@@ -510,7 +527,8 @@ __device__ __forceinline__ void stage_body(const Ring& ring, const TileView& tv,
     }
     __syncwarp();  // the slot fully read before it is refilled
     if (lane == 0) prod.refill(ring, tv, N, rg, hz.stream);
-    stage_steps<kUp, kHalf, kGroup>(ra, rb, rs, rp, rv, rw, first, N, c, amer, active, sout, hz, yh, f);
+    stage_steps<kUp, kHalf, kGroup>(ra, rb, rs, rp, rv, rw, first, c, active, sout,
+                                    stage_policy<kUp>(first, kGroup, N, hz), yh, f);
 }
 
 // One wide stage (kWide middle-region nodes, wide layout).
@@ -524,11 +542,12 @@ __device__ __forceinline__ void stage_body_wide(const Ring& ring, const TileView
     constexpr int kW = rec_width<kTwin>();
     const double* sp_ = reinterpret_cast<const double*>(st) + (kTwin ? lane >> 1 : lane);
     const double2* ss_ = reinterpret_cast<const double2*>(st + kWideP) + lane;
-    double ra[kWide], rb[kWide], rs[kWide], rp[kWide], rv[kWide], rw[kWide];
+    double ra[kWide], rb[kWide], rs[kWide], rv[kWide], rw[kWide];
+    long long rp[kWide];
 #pragma unroll
     for (int k = 0; k < kWide; ++k) {
         const int idx = kUp ? k : kWide - 1 - k;
-        rp[k] = pfree ? 0. : sp_[idx * kW];
+        rp[k] = floor_bits(pfree ? 0. : sp_[idx * kW], amer, first + idx, N);
         const double2 sv = ss_[idx * kTile];
         rv[k] = sv.x;
         rw[k] = sv.y;
@@ -538,7 +557,8 @@ __device__ __forceinline__ void stage_body_wide(const Ring& ring, const TileView
     }
     __syncwarp();
     if (lane == 0) prod.refill(ring, tv, N, rg, hz.stream);
-    stage_steps<kUp, kHalf, kWide>(ra, rb, rs, rp, rv, rw, first, N, c, amer, active, sout, hz, yh, f);
+    stage_steps<kUp, kHalf, kWide>(ra, rb, rs, rp, rv, rw, first, c, active, sout,
+                                   stage_policy<kUp>(first, kWide, N, hz), yh, f);
 }
 
 // A sweep's last stage when it holds fewer than kGroup nodes.  It refills no ring
