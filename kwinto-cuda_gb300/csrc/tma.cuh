@@ -123,4 +123,20 @@ __device__ __forceinline__ void fence_proxy_async_global()
     asm volatile("fence.proxy.async.global;" ::: "memory");
 }
 
+// The same for shared memory: this thread's earlier generic-proxy reads and writes of
+// shared memory are ordered before later async-proxy accesses (a bulk copy that
+// refills the buffer).  A warp barrier alone does not give this order: a refill
+// issued right after __syncwarp() has overwritten a buffer while other lanes' loads
+// of it were still outstanding.
+__device__ __forceinline__ void fence_proxy_async_shared()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Both state spaces at once.
+__device__ __forceinline__ void fence_proxy_async_all()
+{
+    asm volatile("fence.proxy.async;" ::: "memory");
+}
+
 }  // namespace kwg
