@@ -272,9 +272,17 @@ int kwg_mlp_gradients(kwg_mlp* h, const float* d_x, const float* d_t, const floa
 int kwg_mlp_featurize(kwg_mlp* h, const kwg_option* d_opts, int n, float* d_x, uint8_t* d_inside, double* d_base);
 /* Trains on device options with their FD prices (device): premium targets scaled to
  * unit standard deviation, exercise-region floors, Adam with a cosine learning-rate
- * schedule, shuffled minibatches.  *final_loss = mean loss of the last epoch. */
+ * schedule, shuffled minibatches.  The network keeps the parameters of the epoch with
+ * the lowest mean minibatch loss; an epoch whose mean loss is not finite or exceeds
+ * 3x that best returns to the best parameters with fresh Adam moments and halves the
+ * learning rate for the remaining epochs.  *final_loss = the kept epoch's mean loss. */
 int kwg_mlp_train(kwg_mlp* h, const kwg_option* d_opts, const double* d_prices, int n, int epochs, int batch,
                   float lr, uint64_t seed, double* final_loss);
+/* The last kwg_mlp_train run of h: copies min(epochs, cap) per-epoch mean losses to
+ * losses, the kept epoch to *best_epoch (-1 if none) and the number of returns after
+ * a loss spike to *restarts (either may be NULL); returns the epoch count, or -1 for
+ * invalid arguments.  Host only, no device work. */
+int kwg_mlp_train_history(kwg_mlp* h, double* losses, int cap, int* best_epoch, int* restarts);
 /* Network prices of device options (no fallback): max(intrinsic, base + K *
  * premium) for American options; d_inside (may be NULL) flags options inside the
  * training box. */

@@ -50,6 +50,10 @@ struct kwg_mlp {
     __nv_bfloat16 *dy = nullptr, *dyt = nullptr, *dz = nullptr, *dzt = nullptr;
     double* loss = nullptr;
     int* error = nullptr;
+    // the last training run: mean loss of every epoch, the epoch whose parameters
+    // were kept, and how many loss spikes sent it back to them
+    std::vector<double> loss_hist;
+    int best_epoch = -1, restarts = 0;
     // surrogate pricing arena (grow-only), carved by route_layout()
     char* d_arena = nullptr;
     size_t arena_bytes = 0;
@@ -458,19 +462,20 @@ int kwg_mlp_train(kwg_mlp* h, const kwg_option* d_opts, const double* d_prices, 
     const int b_pad = (std::min(batch, n) + 63) / 64 * 64;
     if (int rc = ensure_ws(h, b_pad)) return rc;
     // features, premium targets and exercise-region floors of the whole training set
-    float *X = nullptr, *T = nullptr, *F = nullptr;
+    float *X = nullptr, *T = nullptr, *F = nullptr, *pbest = nullptr;
     double* base = nullptr;
     int32_t* idx = nullptr;
     auto cleanup = [&]() {
         cudaFree(X);
         cudaFree(T);
         cudaFree(F);
+        cudaFree(pbest);
         cudaFree(base);
         cudaFree(idx);
     };
     if (cudaMalloc(&X, (size_t)n * kMlpIn * 4) != cudaSuccess || cudaMalloc(&T, (size_t)n * 4) != cudaSuccess ||
         cudaMalloc(&F, (size_t)n * 4) != cudaSuccess || cudaMalloc(&base, (size_t)n * 8) != cudaSuccess ||
-        cudaMalloc(&idx, (size_t)n * 4) != cudaSuccess) {
+        cudaMalloc(&idx, (size_t)n * 4) != cudaSuccess || cudaMalloc(&pbest, sizeof(float) * kMlpParams) != cudaSuccess) {
         cleanup();
         return mlp_err(h, KWG_ERR_CUDA, "kwg_mlp_train: out of device memory");
     }
@@ -497,7 +502,15 @@ int kwg_mlp_train(kwg_mlp* h, const kwg_option* d_opts, const double* d_prices, 
     const int steps_per_epoch = (n + batch - 1) / batch;
     const long long total = (long long)steps_per_epoch * epochs;
     long long step = 0;
-    double last = 0.;
+    // the parameters of the epoch with the lowest mean loss are kept; an epoch whose
+    // loss is not finite or above kSpike x that best goes back to them with fresh Adam
+    // moments and half the learning rate for the rest of the run
+    constexpr double kSpike = 3.;
+    double best = HUGE_VAL;
+    float lr_scale = 1.f;
+    h->loss_hist.clear();
+    h->best_epoch = -1;
+    h->restarts = 0;
     for (int ep = 0; ep < epochs; ++ep) {
         std::shuffle(order.begin(), order.end(), rng);
         if (cudaMemcpyAsync(idx, order.data(), (size_t)n * 4, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
@@ -518,7 +531,7 @@ int kwg_mlp_train(kwg_mlp* h, const kwg_option* d_opts, const double* d_prices, 
             // Adam with a cosine-decayed learning rate (to 1% of lr)
             ++h->adam_t;
             const double frac = (double)step / std::max(1LL, total - 1);
-            const float lr_t = (float)(lr * (0.01 + 0.99 * 0.5 * (1. + std::cos(M_PI * frac))));
+            const float lr_t = lr_scale * (float)(lr * (0.01 + 0.99 * 0.5 * (1. + std::cos(M_PI * frac))));
             const float b1 = 0.9f, b2 = 0.999f;
             kwg::mlp_launch_adam(h->p, h->g, h->m, h->v, kMlpParams, lr_t, b1, b2, 1e-8f,
                                  1.f - std::pow(b1, (float)h->adam_t), 1.f - std::pow(b2, (float)h->adam_t),
@@ -532,12 +545,54 @@ int kwg_mlp_train(kwg_mlp* h, const kwg_option* d_opts, const double* d_prices, 
             cleanup();
             return mlp_err(h, KWG_ERR_CUDA, "kwg_mlp_train: loss copy failed");
         }
-        last = l / steps_per_epoch;
+        const double mean = l / steps_per_epoch;
+        h->loss_hist.push_back(mean);
+        cudaError_t e = cudaSuccess;
+        if (std::isfinite(mean) && mean < best) {
+            best = mean;
+            h->best_epoch = ep;
+            e = cudaMemcpyAsync(pbest, h->p, sizeof(float) * kMlpParams, cudaMemcpyDeviceToDevice, h->stream);
+        } else if (h->best_epoch >= 0 && !(mean <= kSpike * best)) {
+            ++h->restarts;
+            lr_scale *= 0.5f;
+            h->adam_t = 0;
+            e = cudaMemcpyAsync(h->p, pbest, sizeof(float) * kMlpParams, cudaMemcpyDeviceToDevice, h->stream);
+            if (e == cudaSuccess) e = cudaMemsetAsync(h->m, 0, sizeof(float) * kMlpParams, h->stream);
+            if (e == cudaSuccess) e = cudaMemsetAsync(h->v, 0, sizeof(float) * kMlpParams, h->stream);
+            if (e == cudaSuccess) kwg::mlp_launch_refresh(h->p, h->wb, h->wt, h->stream);
+        }
+        if (e != cudaSuccess) {
+            cleanup();
+            return mlp_err(h, KWG_ERR_CUDA, std::string("kwg_mlp_train: parameter snapshot: ") + cudaGetErrorString(e));
+        }
+    }
+    if (h->best_epoch >= 0 && h->best_epoch != epochs - 1) {
+        // the last epoch was not the best: its parameters give way to the best epoch's
+        if (cudaMemcpyAsync(h->p, pbest, sizeof(float) * kMlpParams, cudaMemcpyDeviceToDevice, h->stream) !=
+            cudaSuccess) {
+            cleanup();
+            return mlp_err(h, KWG_ERR_CUDA, "kwg_mlp_train: parameter restore failed");
+        }
+        kwg::mlp_launch_refresh(h->p, h->wb, h->wt, h->stream);
+    }
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
+        cleanup();
+        return mlp_err(h, KWG_ERR_CUDA, "kwg_mlp_train: final synchronisation failed");
     }
     const int rc = check_error(h);
     cleanup();
-    if (final_loss) *final_loss = last;
+    if (final_loss) *final_loss = h->best_epoch >= 0 ? best : h->loss_hist.back();
     return rc;
+}
+
+int kwg_mlp_train_history(kwg_mlp* h, double* losses, int cap, int* best_epoch, int* restarts)
+{
+    if (!h || cap < 0 || (cap > 0 && !losses)) return -1;
+    const int n = (int)h->loss_hist.size();
+    for (int i = 0; i < std::min(n, cap); ++i) losses[i] = h->loss_hist[i];
+    if (best_epoch) *best_epoch = h->best_epoch;
+    if (restarts) *restarts = h->restarts;
+    return n;
 }
 
 int kwg_mlp_price_device(kwg_mlp* h, const kwg_option* d_opts, int n, double* d_prices, uint8_t* d_inside)

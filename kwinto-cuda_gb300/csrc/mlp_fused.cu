@@ -1,19 +1,25 @@
 // mlp_fused.cu -- surrogate pricing in one persistent tcgen05 kernel: option in,
 // price out, activations never leave the SM.
 //
-// One CTA per SM (128 threads, one option row per thread) keeps the BF16 weights of
-// all layers in shared memory (core-matrix layout, tc.cuh) for its whole life and
-// walks 128-option tiles:
-//   1. each thread computes its option's features and writes the split BF16 row
-//      (hi 0..4, lo 5..9) into the 128 x 16 input tile;
+// One CTA per SM (256 threads: two warpgroups over one option row per thread pair)
+// keeps the BF16 weights of all layers in shared memory (core-matrix layout, tc.cuh)
+// for its whole life and walks 128-option tiles.  Thread t serves row t % 128; the
+// first warpgroup handles accumulator columns 0..63 of its rows, the second 64..127
+// (a warp reads the TMEM lanes of its rank in the warpgroup):
+//   1. the first warpgroup computes each option's features and writes the split BF16
+//      row (hi 0..4, lo 5..9) into the 128 x 16 input tile;
 //   2. thread 0 issues the layer-1 MMA (K = 16) into a 128-column TMEM accumulator;
-//      meanwhile every thread computes its option's analytic base price (FP64);
+//      meanwhile the second warpgroup computes each option's analytic base price
+//      (FP64);
 //   3. layers 2-4: the epilogue reads the accumulator (tcgen05.ld), adds the bias,
 //      applies SiLU and writes the activation as a BF16 pair into the hi and lo
-//      128 x 128 tiles; thread 0 then issues 8 MMAs over hi and 8 over lo with the
-//      same weight operand (the GEMM path's K-doubled [W | W] sums the same terms);
-//   4. the layer-4 epilogue folds the 128 -> 1 head into an FP32 dot product and
-//      writes max(intrinsic, base + K y / y_scale).
+//      128 x 128 tiles, each warpgroup its 64 columns; thread 0 then issues 8 MMAs
+//      over hi and 8 over lo with the same weight operand (the GEMM path's K-doubled
+//      [W | W] sums the same terms);
+//   4. the layer-4 epilogue folds the 128 -> 1 head into an FP32 dot product in
+//      column order (the first warpgroup sums columns 0..63, the second continues
+//      from its partial over 64..127, as the GEMM path's epilogue does) and writes
+//      max(intrinsic, base + K y / y_scale).
 // The arithmetic matches the layer-by-layer path (mlp_gemm.cu) step for step.
 // Every MMA completion wait is bounded; on a timeout the kernel sets *error, waits
 // (bounded) for the MMAs in flight and frees its TMEM.
@@ -31,7 +37,9 @@ namespace kwg {
 
 namespace {
 
-constexpr int kRows = 128;  // options per tile, one per thread
+constexpr int kRows = 128;  // options per tile, one row per thread pair
+constexpr int kThreads = 2 * kRows;
+constexpr int kHalfCols = kMlpWidth / 2;  // accumulator columns per warpgroup
 constexpr int kK1 = 16;     // layer-1 K: features hi 0..4, lo 5..9, zeros
 constexpr uint32_t kW1Bytes = kMlpWidth * kK1 * 2;
 constexpr uint32_t kWBytes = kMlpWidth * kMlpWidth * 2;
@@ -44,7 +52,8 @@ constexpr uint32_t kOffAhi = kOffX + kXBytes;
 constexpr uint32_t kOffAlo = kOffAhi + kABytes;
 constexpr uint32_t kOffBias = kOffAlo + kABytes;            // 4 x 128 FP32
 constexpr uint32_t kOffHead = kOffBias + 4 * kMlpWidth * 4;  // 128 FP32 (BF16 head weights, widened)
-constexpr uint32_t kOffMisc = kOffHead + kMlpWidth * 4;      // mbarrier, TMEM address
+constexpr uint32_t kOffY = kOffHead + kMlpWidth * 4;         // 128 FP32: head partial sums
+constexpr uint32_t kOffMisc = kOffY + kRows * 4;             // mbarrier, TMEM address
 constexpr uint32_t kSmemBytes = kOffMisc + 64;
 constexpr uint32_t kTmemCols = 128;
 static_assert(kOffX % 1024 == 0 && kOffAhi % 1024 == 0 && kOffAlo % 1024 == 0, "operand tiles 1 KB aligned");
@@ -56,17 +65,19 @@ __device__ __forceinline__ void store_core(unsigned char* base, int kc, int row,
 
 }  // namespace
 
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(kThreads, 1)
     mlp_price_fused(const kwg_option* __restrict__ opts, int n, MlpBox box, const __nv_bfloat16* __restrict__ wb,
                     const float* __restrict__ params, float y_scale, double* __restrict__ prices,
                     uint8_t* __restrict__ inside, int* __restrict__ error)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
     const int tid = threadIdx.x, warp = tid / 32;
+    const int row = tid % kRows, half = tid / kRows;
     uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kOffMisc);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + kOffMisc + 8);
     float* bias = reinterpret_cast<float*>(sm + kOffBias);
     float* head = reinterpret_cast<float*>(sm + kOffHead);
+    float* ypart = reinterpret_cast<float*>(sm + kOffY);
 
     // resident weights: W1 = columns 0..15 of forward slot 0 ([128][64]); W2..W4 =
     // columns 0..127 of slots 1..3 ([128][256]); biases and the head row
@@ -97,7 +108,8 @@ __global__ void __launch_bounds__(128, 1)
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *tslot;
-    const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's 32 lanes
+    // this warp's 32 lanes (its rank in the warpgroup) and its warpgroup's columns
+    const uint32_t tl = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(half * kHalfCols);
     const uint32_t idesc = tc::idesc_bf16_f32(kRows, kMlpWidth);
     const uint32_t sx = smem_addr(sm + kOffX), sw1 = smem_addr(sm + kOffW1), sw = smem_addr(sm + kOffW);
     const uint32_t shi = smem_addr(sm + kOffAhi), slo = smem_addr(sm + kOffAlo);
@@ -105,7 +117,7 @@ __global__ void __launch_bounds__(128, 1)
     bool ok = true, pending = false;
 
     for (int tile = blockIdx.x; tile * kRows < n; tile += gridDim.x) {
-        const int i = tile * kRows + tid;
+        const int i = tile * kRows + row;
         const bool real = i < n;
         kwg_option o = {};
         float f[kMlpIn] = {0.f, 0.f, 0.f, 0.f, 0.f};
@@ -114,11 +126,11 @@ __global__ void __launch_bounds__(128, 1)
             o = opts[i];
             features(o, box, f, in);
         }
-        {
+        if (half == 0) {
             __align__(16) __nv_bfloat16 xr[kK1];
             split_features<kK1>(f, xr);
-            store_core(sm + kOffX, kK1, tid, 0, xr);
-            store_core(sm + kOffX, kK1, tid, 8, xr + 8);
+            store_core(sm + kOffX, kK1, row, 0, xr);
+            store_core(sm + kOffX, kK1, row, 8, xr + 8);
         }
         tc::fence_proxy_async_smem();
         tc::fence_before_sync();
@@ -130,9 +142,9 @@ __global__ void __launch_bounds__(128, 1)
             tc::commit(smem_addr(mbar));
         }
         pending = true;
-        const double base = real ? base_price(o) : 0.;  // FP64, overlapped with the MMA
+        const double base = (half == 1 && real) ? base_price(o) : 0.;  // FP64, overlapped with the MMA
 
-        float y = 0.f;
+        float y = 0.f, a4[kHalfCols];  // layer-4 activations of this warpgroup's columns
         for (int l = 0; l < 4; ++l) {
             ok = mbar_wait(mbar, phase) && ok;
             phase ^= 1u;
@@ -140,9 +152,11 @@ __global__ void __launch_bounds__(128, 1)
             if (!ok) break;
             pending = false;
             tc::fence_after_sync();
-            for (int c = 0; c < kMlpWidth; c += 32) {
+#pragma unroll
+            for (int cc = 0; cc < kHalfCols; cc += 32) {
+                const int c = half * kHalfCols + cc;  // the accumulator column
                 float v[32];
-                tc::tmem_ld32(tl + (uint32_t)c, v);
+                tc::tmem_ld32(tl + (uint32_t)cc, v);
                 if (l < 3) {
                     __align__(16) __nv_bfloat16 hi[32], lo[32];
 #pragma unroll
@@ -153,15 +167,29 @@ __global__ void __launch_bounds__(128, 1)
                     }
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
-                        store_core(sm + kOffAhi, kMlpWidth, tid, c + 8 * q, hi + 8 * q);
-                        store_core(sm + kOffAlo, kMlpWidth, tid, c + 8 * q, lo + 8 * q);
+                        store_core(sm + kOffAhi, kMlpWidth, row, c + 8 * q, hi + 8 * q);
+                        store_core(sm + kOffAlo, kMlpWidth, row, c + 8 * q, lo + 8 * q);
                     }
                 } else {
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) y = fmaf(head[c + j], silu_f(v[j] + bias[3 * kMlpWidth + c + j]), y);
+                    for (int j = 0; j < 32; ++j) a4[cc + j] = silu_f(v[j] + bias[3 * kMlpWidth + c + j]);
                 }
             }
-            if (l == 3) break;
+            if (l == 3) {
+                // the head in column order: columns 0..63, then 64..127 from that partial
+                if (half == 0) {
+#pragma unroll
+                    for (int j = 0; j < kHalfCols; ++j) y = fmaf(head[j], a4[j], y);
+                    ypart[row] = y;
+                }
+                __syncthreads();
+                if (half == 1) {
+                    y = ypart[row];
+#pragma unroll
+                    for (int j = 0; j < kHalfCols; ++j) y = fmaf(head[kHalfCols + j], a4[j], y);
+                }
+                break;
+            }
             // layer l + 2: activations (hi, then lo) x W_{l+2}
             tc::fence_proxy_async_smem();
             tc::fence_before_sync();
@@ -182,7 +210,7 @@ __global__ void __launch_bounds__(128, 1)
             pending = true;
         }
         if (!ok) break;
-        if (real) {
+        if (half == 1 && real) {
             const double v = base + o.k * (double)((y + head_b) / y_scale);
             prices[i] = o.e ? fmax(v, intrinsic(o)) : v;
             if (inside) inside[i] = in ? 1 : 0;
@@ -218,7 +246,7 @@ cudaError_t mlp_launch_price_fused(const kwg_option* opts, int n, const MlpBox& 
     if (const cudaError_t e = mlp_prepare_device(); e != cudaSuccess) return e;
     const int tiles = (n + kRows - 1) / kRows;
     const int grid = tiles < sms ? tiles : sms;
-    mlp_price_fused<<<grid, kRows, kSmemBytes, st>>>(opts, n, box, wb, params, y_scale, prices, inside, error);
+    mlp_price_fused<<<grid, kThreads, kSmemBytes, st>>>(opts, n, box, wb, params, y_scale, prices, inside, error);
     return cudaGetLastError();
 }
 

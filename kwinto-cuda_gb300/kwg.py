@@ -161,6 +161,8 @@ def lib() -> ctypes.CDLL:
     L.kwg_mlp_featurize.argtypes = [vp, vp, i32, vp, vp, vp]
     L.kwg_mlp_train.argtypes = [vp, vp, vp, i32, i32, i32, f32, u64, ctypes.POINTER(dbl)]
     L.kwg_mlp_price_device.argtypes = [vp, vp, i32, vp, vp]
+    L.kwg_mlp_train_history.argtypes = [vp, vp, i32, ctypes.POINTER(i32), ctypes.POINTER(i32)]
+    L.kwg_mlp_train_history.restype = i32
     L.kwg_surrogate_price.argtypes = [vp, vp, vp, sz, ctypes.POINTER(Fd1dParams), dbl, u64, dp, dp,
                                       ctypes.POINTER(Audit)]
     for name in ("set_params", "get_params", "forward", "gradients", "featurize", "train", "price_device"):
@@ -382,6 +384,17 @@ class Surrogate:
         self._check(self._L.kwg_mlp_train(self.ptr, d_opts, d_prices, n, epochs, batch, lr, seed,
                                           ctypes.byref(loss)))
         return loss.value
+
+    def train_history(self) -> dict:
+        """The last train() run: per-epoch mean losses, the epoch whose parameters the
+        network kept, and the returns to them after a loss spike."""
+        best, restarts = ctypes.c_int(0), ctypes.c_int(0)
+        n = self._L.kwg_mlp_train_history(self.ptr, None, 0, ctypes.byref(best), ctypes.byref(restarts))
+        if n < 0:
+            raise RuntimeError("kwg_mlp_train_history: invalid arguments")
+        losses = np.zeros(n)
+        self._L.kwg_mlp_train_history(self.ptr, losses.ctypes.data if n else None, n, None, None)
+        return {"losses": losses, "best_epoch": best.value, "restarts": restarts.value}
 
     def price_device(self, d_opts: int, n: int, d_prices: int, d_inside: int = 0):
         self._check(self._L.kwg_mlp_price_device(self.ptr, d_opts, n, d_prices, d_inside or None))

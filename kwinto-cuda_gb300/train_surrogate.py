@@ -83,9 +83,12 @@ def train(ctx, n: int = 2_000_000, grid: int = 1024, epochs: int = 150, batch: i
     t0 = time.perf_counter()
     loss = net.train(d_o.data_ptr(), d_p.data_ptr(), n, epochs, batch, lr, seed)
     t_train = time.perf_counter() - t0
+    hist = net.train_history()
     report = evaluate(net, ctx, test, grid)
     meta = {"n_train": n, "grid": grid, "epochs": epochs, "batch": batch, "lr": lr, "seed": seed,
-            "label_s": t_label, "train_s": t_train, "final_loss": loss, "heldout": report}
+            "label_s": t_label, "train_s": t_train, "final_loss": loss, "kept_epoch": hist["best_epoch"],
+            "spike_restarts": hist["restarts"], "last_epoch_loss": float(hist["losses"][-1]),
+            "heldout": report}
     del d_o, d_p
     return net, meta
 

@@ -187,6 +187,19 @@ def test_training_reduces_loss(trained):
     assert after < 5e-3  # targets are scaled to unit standard deviation
 
 
+def test_training_keeps_the_best_epoch(trained):
+    """The training history: one mean loss per epoch, the kept epoch is the one with
+    the lowest loss, and the loss train() reports is that epoch's."""
+    s, _, _, last = trained
+    h = s.train_history()
+    assert len(h["losses"]) == 60
+    assert np.isfinite(h["losses"]).all()
+    assert h["best_epoch"] == int(np.argmin(h["losses"]))
+    assert last == h["losses"][h["best_epoch"]]
+    assert h["restarts"] >= 0
+    assert h["losses"][h["best_epoch"]] < 1e-2 * h["losses"][0]
+
+
 def test_trained_network_beats_analytic_prices(trained, ctx):
     """What the network gains: on fresh options, the surrogate price (analytic base +
     learned premium) is far closer to FD64 than the same method without the network,
