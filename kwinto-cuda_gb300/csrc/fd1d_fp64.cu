@@ -38,8 +38,8 @@
 //     P  [node][32]     payoff
 //     S  [node][32][2]  state (V, h|f), one 16-byte load/store per lane
 // A sweep streams them in stages of consecutive nodes (one mbarrier, one to three
-// bulk copies per stage): 2 kGroup nodes in the middle region, where the coefficients
-// are not read, kGroup nodes elsewhere.  Where the payoff of every lane of the tile
+// bulk copies per stage): 2 G nodes in the middle region, where the coefficients are
+// not read, G nodes elsewhere (G = 8, or 16 for launches with few warps per SM).  Where the payoff of every lane of the tile
 // is exactly +0 (the out-of-the-money
 // side of a tile of puts only or calls only; all nodes of European PDEs, which never
 // project) the payoff is not read either: the projection there is max(V, +0).
@@ -59,7 +59,6 @@ namespace {
 
 constexpr int kCoef = 3;                                   // coefficients per node and sweep
 constexpr int kConsts = 6;                                 // nh l 1/e uh m 1/d in the middle
-constexpr int kGroup = 8;                                  // nodes per stage
 constexpr uint32_t kNodeCoefBytes = kCoef * kTile * 8;    // 768 B
 constexpr uint32_t kNodePBytes = kTile * 8;               // 256 B
 constexpr uint32_t kNodeSBytes = 2 * kTile * 8;           // 512 B
@@ -306,23 +305,38 @@ __global__ void __launch_bounds__(128) fd1d_setup_fp64(const PdeBatch b, Fd1dSha
 
 namespace {
 
-// Ring of stage slots in shared memory; a slot holds kGroup consecutive nodes of one
-// sweep -- coefficients [kGroup][3][32], payoff [kGroup][32], state [kGroup][32][2] --
-// or, in the middle region, 2 kGroup nodes of payoff and state (see kWide below).
-// Stage visits are numbered per warp (q); visit q uses slot q % kRing with mbarrier
-// parity (q / kRing) & 1.
-// 12 KB slots, double-buffered: 24 KB per warp keeps >= 7 single-warp blocks per SM
-// (the 1024 tiles of a 32768-option batch in one wave).  Measured on the 32768-option
-// 1024 x 1024 batch with uniform stages (launch ms, nodes x ring): 4x4 246, 6x3 236,
-// 7x2 223, 8x2 219, 10x2 401 (6 blocks per SM: a second wave), 2x8 314; 16-node
-// middle stages in the same slots then 199.
+// Ring of stage slots in shared memory; a slot holds G consecutive nodes of one sweep
+// -- coefficients [G][3][32], payoff [G][32], state [G][32][2] -- or, in the middle
+// region, 2 G nodes of payoff and state (wide stages).  Stage visits are numbered per
+// warp (q); visit q uses slot q % kRing with mbarrier parity (q / kRing) & 1.
+// Small stages (G = 8): 12 KB slots, double-buffered: 24 KB per warp keeps >= 7
+// single-warp blocks per SM (the 1024 tiles of a 32768-option batch in one wave).
+// Measured on the 32768-option 1024 x 1024 batch with uniform stages (launch ms,
+// nodes x ring): 4x4 246, 6x3 236, 7x2 223, 8x2 219, 10x2 401 (6 blocks per SM: a
+// second wave), 2x8 314; 16-node middle stages in the same slots then 199.
+// Big stages (G = 16): 24 KB slots, 48 KB per warp, for launches that cap the
+// residency (one 4-warp block per SM: one warp per scheduler).  Each stage boundary
+// (mbarrier wait, fence, warp barrier, refill) stalls the warp's FMA chain, and a
+// warp alone on its scheduler has no other warp to fill that time: a lone warp on
+// 2048-node grids takes 261 cycles per node-step with big stages against 291 with
+// small ones.  The stage is loaded into registers in chunks of 8 (coefficient
+// stages) or 16 (wide stages) nodes, so the register arrays stay those of the small
+// stages.
 constexpr int kRing = 2;
-constexpr uint32_t kStageCoef = kGroup * kNodeCoefBytes;  // 6 KB
-constexpr uint32_t kStageP = kGroup * kNodePBytes;        // 2 KB
-constexpr uint32_t kStageS = kGroup * kNodeSBytes;        // 4 KB
-constexpr uint32_t kStageBytes = kStageCoef + kStageP + kStageS;
-// one warp's ring and mbarriers, rounded so the next warp's stages stay aligned
-constexpr size_t kSolveSmem = (kRing * kStageBytes + kRing * sizeof(uint64_t) + 127) / 128 * 128;
+template <bool kBig>
+struct Geo {
+    static constexpr int kGroup = kBig ? 16 : 8;  // nodes of a coefficient stage
+    static constexpr int kWide = 2 * kGroup;      // nodes of a wide (middle-region) stage
+    static constexpr int kSubC = 8, kSubW = 16;   // nodes per register chunk
+    static constexpr uint32_t kStageCoef = kGroup * kNodeCoefBytes;
+    static constexpr uint32_t kStageP = kGroup * kNodePBytes;
+    static constexpr uint32_t kStageBytes = kStageCoef + kStageP + kGroup * kNodeSBytes;
+    static constexpr uint32_t kWideP = kWide * kNodePBytes;  // wide stage: payoff [0, kWideP), state after it
+    // one warp's ring and mbarriers, rounded so the next warp's stages stay aligned
+    static constexpr size_t kSolveSmem = (kRing * kStageBytes + kRing * sizeof(uint64_t) + 127) / 128 * 128;
+    static_assert(kWideP + kWide * kNodeSBytes == kStageBytes, "a wide stage fills one slot");
+    static_assert(kGroup % kSubC == 0 && kWide % kSubW == 0, "whole register chunks");
+};
 constexpr int kMaxBlockWarps = 4;
 // share of the L2 given to the state lines at the sweep ends (evict-last)
 constexpr double kKeepShare = 0.5;
@@ -353,12 +367,9 @@ struct Hints {
 };
 
 // Wide stages: in the middle region a stage needs no coefficients, so the same slot
-// holds 2 kGroup nodes -- payoff [0, kWideP), state after it -- instead of kGroup
-// nodes with coefficients [0, kStageCoef), payoff, state.  Half the stage overhead
-// (mbarrier wait, warp sync, refill) per node where most nodes are.
-constexpr int kWide = 2 * kGroup;
-constexpr uint32_t kWideP = kWide * kNodePBytes;  // 4 KB
-static_assert(kWideP + kWide * kNodeSBytes == kStageBytes, "a wide stage fills one slot");
+// holds 2 G nodes -- payoff [0, kWideP), state after it -- instead of G nodes with
+// coefficients [0, kStageCoef), payoff, state.  Half the stage overhead (mbarrier
+// wait, warp sync, refill) per node where most nodes are.
 
 // A stage of a sweep: nodes [first, first + count), ascending in memory.
 struct Stage {
@@ -371,9 +382,10 @@ struct Stage {
 // The stage starting at cursor `cur` (kUp: its lowest node, else its highest).  Wide
 // where kWide nodes from the cursor lie in the middle region; else kGroup nodes, fewer
 // only at the sweep's end.  Producer and consumer walk the same sequence.
-template <bool kUp>
+template <bool kUp, bool kBig>
 __device__ __forceinline__ Stage stage_at(int cur, int N, const Ranges& rg)
 {
+    constexpr int kGroup = Geo<kBig>::kGroup, kWide = Geo<kBig>::kWide;
     Stage s;
     if (kUp) {
         s.wide = cur >= rg.lo && cur + kWide - 1 <= rg.hi;
@@ -421,9 +433,12 @@ __device__ __forceinline__ unsigned long long stage_bytes(const Stage& s, bool t
 
 // Issues stage visit q for stage sg of this tile.  Twin tiles copy half-width
 // coefficient and payoff records into the front of the same slot areas.
-template <bool kUp, bool kTwin>
+template <bool kUp, bool kTwin, bool kBig>
 __device__ __forceinline__ void issue(const Ring& r, uint32_t q, const TileView& tv, const Stage& sg, uint64_t pol)
 {
+    using G = Geo<kBig>;
+    constexpr uint32_t kStageBytes = G::kStageBytes, kStageCoef = G::kStageCoef, kStageP = G::kStageP,
+                       kWideP = G::kWideP;
     constexpr int kW = rec_width<kTwin>();
     const int s = (int)(q % kRing);
     unsigned char* st = r.stage + (size_t)s * kStageBytes;
@@ -438,15 +453,15 @@ __device__ __forceinline__ void issue(const Ring& r, uint32_t q, const TileView&
 
 // The refilling side of a sweep, run by lane 0: the next stage to issue and its
 // visit number.
-template <bool kUp, bool kTwin>
+template <bool kUp, bool kTwin, bool kBig>
 struct Producer {
     int cur;
     uint32_t next;
     __device__ __forceinline__ void refill(const Ring& ring, const TileView& tv, int N, const Ranges& rg, uint64_t pol)
     {
         if (sweep_done<kUp>(cur, N)) return;
-        const Stage sg = stage_at<kUp>(cur, N, rg);
-        issue<kUp, kTwin>(ring, next, tv, sg, pol);
+        const Stage sg = stage_at<kUp, kBig>(cur, N, rg);
+        issue<kUp, kTwin, kBig>(ring, next, tv, sg, pol);
         cur = stage_after<kUp>(cur, sg);
         ++next;
     }
@@ -497,8 +512,8 @@ __device__ __forceinline__ uint64_t stage_policy(int first, int count, int N, co
     return keep ? hz.keep : hz.stream;
 }
 
-// One full kGroup-node stage: loads it into registers, runs its node-steps, then lets
-// lane 0 refill the slot.  The refill is a bulk copy (async proxy) into memory the
+// One full G-node stage: loads it into registers (in chunks of kSubC nodes), runs its
+// node-steps, then lets lane 0 refill the slot.  The refill is a bulk copy (async proxy) into memory the
 // lanes have just read (generic proxy): every lane fences its reads before the warp
 // barrier that precedes the refill.  Refilling after the node-steps instead of
 // before them also keeps lane 0's issue work off the start of the FMA chain (on the
@@ -506,82 +521,96 @@ __device__ __forceinline__ uint64_t stage_policy(int first, int count, int N, co
 // ahead of the node-steps, which raced).  kCompact: the stage lies in the middle
 // region (coefficients ca, cb, cs).  No per-node guard: the unrolled stage is one
 // block the scheduler interleaves across nodes.
-template <bool kUp, bool kHalf, bool kCompact, bool kTwin>
-__device__ __forceinline__ void stage_body(const Ring& ring, const TileView& tv, Producer<kUp, kTwin>& prod, int N,
-                                           const Ranges& rg, int first, bool pfree, const unsigned char* st, int lane,
-                                           double ca, double cb, double cs, double c, bool amer, bool active,
-                                           double2* sout, const Hints& hz, double& yh, double& f)
+template <bool kUp, bool kHalf, bool kCompact, bool kTwin, bool kBig>
+__device__ __forceinline__ void stage_body(const Ring& ring, const TileView& tv, Producer<kUp, kTwin, kBig>& prod,
+                                           int N, const Ranges& rg, int first, bool pfree, const unsigned char* st,
+                                           int lane, double ca, double cb, double cs, double c, bool amer,
+                                           bool active, double2* sout, const Hints& hz, double& yh, double& f)
 {
+    using G = Geo<kBig>;
+    constexpr int kGroup = G::kGroup, kSub = G::kSubC;
     constexpr int kW = rec_width<kTwin>();
     const int rl = kTwin ? lane >> 1 : lane;  // this lane's entry of the records
     const double* sc_ = reinterpret_cast<const double*>(st) + rl;
-    const double* sp_ = reinterpret_cast<const double*>(st + kStageCoef) + rl;
-    const double2* ss_ = reinterpret_cast<const double2*>(st + kStageCoef + kStageP) + lane;
-    double ra[kGroup], rb[kGroup], rs[kGroup], rv[kGroup], rw[kGroup];
-    long long rp[kGroup];
+    const double* sp_ = reinterpret_cast<const double*>(st + G::kStageCoef) + rl;
+    const double2* ss_ = reinterpret_cast<const double2*>(st + G::kStageCoef + G::kStageP) + lane;
 #pragma unroll
-    for (int k = 0; k < kGroup; ++k) {
-        const int idx = kUp ? k : kGroup - 1 - k;  // processing order within the stage
-        rp[k] = floor_bits(pfree ? 0. : sp_[idx * kW], amer, first + idx, N);
-        const double2 sv = ss_[idx * kTile];
-        rv[k] = sv.x;
-        rw[k] = sv.y;
-        ra[k] = kCompact ? ca : sc_[(idx * kCoef + 0) * kW];
-        rb[k] = kCompact ? cb : sc_[(idx * kCoef + 1) * kW];
-        rs[k] = kCompact ? cs : sc_[(idx * kCoef + 2) * kW];
+    for (int h = 0; h < kGroup / kSub; ++h) {
+        // chunk h in processing order: nodes [cf, cf + kSub)
+        const int cf = kUp ? first + h * kSub : first + kGroup - kSub - h * kSub;
+        double ra[kSub], rb[kSub], rs[kSub], rv[kSub], rw[kSub];
+        long long rp[kSub];
+#pragma unroll
+        for (int k = 0; k < kSub; ++k) {
+            const int idx = (cf - first) + (kUp ? k : kSub - 1 - k);  // node within the stage
+            rp[k] = floor_bits(pfree ? 0. : sp_[idx * kW], amer, first + idx, N);
+            const double2 sv = ss_[idx * kTile];
+            rv[k] = sv.x;
+            rw[k] = sv.y;
+            ra[k] = kCompact ? ca : sc_[(idx * kCoef + 0) * kW];
+            rb[k] = kCompact ? cb : sc_[(idx * kCoef + 1) * kW];
+            rs[k] = kCompact ? cs : sc_[(idx * kCoef + 2) * kW];
+        }
+        stage_steps<kUp, kHalf, kSub>(ra, rb, rs, rp, rv, rw, cf, c, active, sout,
+                                      stage_policy<kUp>(cf, kSub, N, hz), yh, f);
     }
-    stage_steps<kUp, kHalf, kGroup>(ra, rb, rs, rp, rv, rw, first, c, active, sout,
-                                    stage_policy<kUp>(first, kGroup, N, hz), yh, f);
     fence_proxy_async_shared();  // this lane's reads of the slot precede the refill
     __syncwarp();
     if (lane == 0) prod.refill(ring, tv, N, rg, hz.stream);
 }
 
-// One wide stage (kWide middle-region nodes, wide layout).
-template <bool kUp, bool kHalf, bool kTwin>
-__device__ __forceinline__ void stage_body_wide(const Ring& ring, const TileView& tv, Producer<kUp, kTwin>& prod,
-                                                int N, const Ranges& rg, int first, bool pfree,
-                                                const unsigned char* st, int lane, double ca, double cb, double cs,
-                                                double c, bool amer, bool active, double2* sout, const Hints& hz,
-                                                double& yh, double& f)
+// One wide stage (kWide middle-region nodes, wide layout, chunks of kSubW nodes).
+template <bool kUp, bool kHalf, bool kTwin, bool kBig>
+__device__ __forceinline__ void stage_body_wide(const Ring& ring, const TileView& tv,
+                                                Producer<kUp, kTwin, kBig>& prod, int N, const Ranges& rg, int first,
+                                                bool pfree, const unsigned char* st, int lane, double ca, double cb,
+                                                double cs, double c, bool amer, bool active, double2* sout,
+                                                const Hints& hz, double& yh, double& f)
 {
+    using G = Geo<kBig>;
+    constexpr int kWide = G::kWide, kSub = G::kSubW;
     constexpr int kW = rec_width<kTwin>();
     const double* sp_ = reinterpret_cast<const double*>(st) + (kTwin ? lane >> 1 : lane);
-    const double2* ss_ = reinterpret_cast<const double2*>(st + kWideP) + lane;
-    double ra[kWide], rb[kWide], rs[kWide], rv[kWide], rw[kWide];
-    long long rp[kWide];
+    const double2* ss_ = reinterpret_cast<const double2*>(st + G::kWideP) + lane;
 #pragma unroll
-    for (int k = 0; k < kWide; ++k) {
-        const int idx = kUp ? k : kWide - 1 - k;
-        rp[k] = floor_bits(pfree ? 0. : sp_[idx * kW], amer, first + idx, N);
-        const double2 sv = ss_[idx * kTile];
-        rv[k] = sv.x;
-        rw[k] = sv.y;
-        ra[k] = ca;
-        rb[k] = cb;
-        rs[k] = cs;
+    for (int h = 0; h < kWide / kSub; ++h) {
+        const int cf = kUp ? first + h * kSub : first + kWide - kSub - h * kSub;
+        double ra[kSub], rb[kSub], rs[kSub], rv[kSub], rw[kSub];
+        long long rp[kSub];
+#pragma unroll
+        for (int k = 0; k < kSub; ++k) {
+            const int idx = (cf - first) + (kUp ? k : kSub - 1 - k);
+            rp[k] = floor_bits(pfree ? 0. : sp_[idx * kW], amer, first + idx, N);
+            const double2 sv = ss_[idx * kTile];
+            rv[k] = sv.x;
+            rw[k] = sv.y;
+            ra[k] = ca;
+            rb[k] = cb;
+            rs[k] = cs;
+        }
+        stage_steps<kUp, kHalf, kSub>(ra, rb, rs, rp, rv, rw, cf, c, active, sout,
+                                      stage_policy<kUp>(cf, kSub, N, hz), yh, f);
     }
-    stage_steps<kUp, kHalf, kWide>(ra, rb, rs, rp, rv, rw, first, c, active, sout,
-                                   stage_policy<kUp>(first, kWide, N, hz), yh, f);
     fence_proxy_async_shared();
     __syncwarp();
     if (lane == 0) prod.refill(ring, tv, N, rg, hz.stream);
 }
 
-// A sweep's last stage when it holds fewer than kGroup nodes.  It refills no ring
-// slot (no later stage), so it reads shared memory node by node in a rolled loop
-// and holds no stage in registers.
-template <bool kUp, bool kHalf, bool kTwin>
+// A sweep's last stage when it holds fewer than G nodes.  It refills no ring slot (no
+// later stage), so it reads shared memory node by node in a rolled loop and holds no
+// stage in registers.
+template <bool kUp, bool kHalf, bool kTwin, bool kBig>
 __device__ __forceinline__ void tail_stage(int first, int count, bool compact, bool pfree, const unsigned char* st,
                                            int lane, double ca, double cb, double cs, double c, bool amer,
                                            bool active, int N, double2* sout, const Hints& hz, double& yh,
                                            double& f)
 {
+    using G = Geo<kBig>;
     constexpr int kW = rec_width<kTwin>();
     const int rl = kTwin ? lane >> 1 : lane;
     const double* sc_ = reinterpret_cast<const double*>(st) + rl;
-    const double* sp_ = reinterpret_cast<const double*>(st + kStageCoef) + rl;
-    const double2* ss_ = reinterpret_cast<const double2*>(st + kStageCoef + kStageP) + lane;
+    const double* sp_ = reinterpret_cast<const double*>(st + G::kStageCoef) + rl;
+    const double2* ss_ = reinterpret_cast<const double2*>(st + G::kStageCoef + G::kStageP) + lane;
 #pragma unroll 1
     for (int k = 0; k < count; ++k) {
         const int idx = kUp ? k : count - 1 - k;
@@ -602,16 +631,17 @@ __device__ __forceinline__ void tail_stage(int first, int count, bool compact, b
 
 // One sweep over this warp's tile.  Returns the stage visits it consumed, or -1 on a
 // wait timeout (copies in flight already drained).
-template <bool kUp, bool kHalf, bool kTwin>
+template <bool kUp, bool kHalf, bool kTwin, bool kBig>
 __device__ __forceinline__ int sweep(const Ring& ring, uint32_t q, const TileView& tv, int lane, int N,
                                      const Ranges& rg, const double* cst, double c, bool amer, bool active,
                                      const Hints& hz, int* err)
 {
+    using G = Geo<kBig>;
     // the previous sweep's stores, and the lanes' reads of the slots its last stages
     // used, are ordered before the bulk copies that refill them
     fence_proxy_async_all();
     __syncwarp();
-    Producer<kUp, kTwin> prod{sweep_first<kUp>(N), q};
+    Producer<kUp, kTwin, kBig> prod{sweep_first<kUp>(N), q};
     if (lane == 0)
         for (int i = 0; i < kRing; ++i) prod.refill(ring, tv, N, rg, hz.stream);
     // middle-region constants: UP uses (nh, l, 1/e), DOWN (uh, m, 1/d)
@@ -630,19 +660,19 @@ __device__ __forceinline__ int sweep(const Ring& ring, uint32_t q, const TileVie
             __syncwarp();
             return -1;
         }
-        const Stage sg = stage_at<kUp>(cur, N, rg);
-        const unsigned char* st = ring.stage + (size_t)s * kStageBytes;
+        const Stage sg = stage_at<kUp, kBig>(cur, N, rg);
+        const unsigned char* st = ring.stage + (size_t)s * G::kStageBytes;
         if (sg.wide)
-            stage_body_wide<kUp, kHalf, kTwin>(ring, tv, prod, N, rg, sg.first, sg.pfree, st, lane, ca, cb, cs, c,
+            stage_body_wide<kUp, kHalf, kTwin, kBig>(ring, tv, prod, N, rg, sg.first, sg.pfree, st, lane, ca, cb, cs, c,
                                                amer, active, sout, hz, yh, f);
-        else if (sg.count == kGroup && sg.compact)
-            stage_body<kUp, kHalf, true, kTwin>(ring, tv, prod, N, rg, sg.first, sg.pfree, st, lane, ca, cb, cs, c,
+        else if (sg.count == G::kGroup && sg.compact)
+            stage_body<kUp, kHalf, true, kTwin, kBig>(ring, tv, prod, N, rg, sg.first, sg.pfree, st, lane, ca, cb, cs, c,
                                                 amer, active, sout, hz, yh, f);
-        else if (sg.count == kGroup)
-            stage_body<kUp, kHalf, false, kTwin>(ring, tv, prod, N, rg, sg.first, sg.pfree, st, lane, ca, cb, cs, c,
+        else if (sg.count == G::kGroup)
+            stage_body<kUp, kHalf, false, kTwin, kBig>(ring, tv, prod, N, rg, sg.first, sg.pfree, st, lane, ca, cb, cs, c,
                                                  amer, active, sout, hz, yh, f);
         else
-            tail_stage<kUp, kHalf, kTwin>(sg.first, sg.count, sg.compact, sg.pfree, st, lane, ca, cb, cs, c, amer,
+            tail_stage<kUp, kHalf, kTwin, kBig>(sg.first, sg.count, sg.compact, sg.pfree, st, lane, ca, cb, cs, c, amer,
                                           active, N, sout, hz, yh, f);
         cur = stage_after<kUp>(cur, sg);
     }
@@ -655,22 +685,23 @@ __device__ __forceinline__ int sweep(const Ring& ring, uint32_t q, const TileVie
 // the launch) and runs all tDim-1 steps of its 32 PDEs.  A block holds 1, 2 or 4
 // independent warps (32 options each; each warp has its own ring); the block size is
 // a tuned launch parameter.  The sweeps stream through a 2-deep ring of stages in
-// shared memory filled by the TMA engine (16 nodes in the middle region, 8 with
-// coefficients elsewhere); V and h|f are
+// shared memory filled by the TMA engine (2 G nodes in the middle region, G with
+// coefficients elsewhere; G = 8, or 16 with kBig); V and h|f are
 // written back with 16-byte stores, L2 evict-last for the last sh.keep_nodes nodes of a
 // sweep (read back first by the next one) and evict-first otherwise.  If a ring wait expires,
 // tile_counter[1] is set, the warp drains its copies in flight and leaves; the
 // interpolation kernel then marks every option with KWG_STATUS_DEVICE_TIMEOUT.
 // tile_counter[2..3] accumulates (64-bit) the bytes the launch reads and writes.
-// kHalf: theta = 1/2 (c = 1).
-template <bool kHalf>
+// kHalf: theta = 1/2 (c = 1).  kBig: the big stage geometry (Geo).
+template <bool kHalf, bool kBig>
 __global__ void __launch_bounds__(32 * kMaxBlockWarps)
     fd1d_solve_fp64(const PdeBatch b, Fd1dShape sh, double* __restrict__ base, int* __restrict__ tile_counter)
 {
+    using G = Geo<kBig>;
     extern __shared__ __align__(128) unsigned char smem[];
     Ring ring;
-    ring.stage = smem + (size_t)(threadIdx.x >> 5) * kSolveSmem;
-    ring.bar = reinterpret_cast<uint64_t*>(ring.stage + kRing * kStageBytes);
+    ring.stage = smem + (size_t)(threadIdx.x >> 5) * G::kSolveSmem;
+    ring.bar = reinterpret_cast<uint64_t*>(ring.stage + kRing * G::kStageBytes);
     const int lane = threadIdx.x & 31;
     if (lane == 0) {
         for (int s = 0; s < kRing; ++s) mbar_init(&ring.bar[s], 1);
@@ -716,12 +747,12 @@ __global__ void __launch_bounds__(32 * kMaxBlockWarps)
             // bytes this tile moves per sweep: the stages' bulk reads + the state stores
             unsigned long long per_up = 0, per_dn = 0;
             for (int cur = sweep_first<true>(N); !sweep_done<true>(cur, N);) {
-                const Stage sg = stage_at<true>(cur, N, rg);
+                const Stage sg = stage_at<true, kBig>(cur, N, rg);
                 per_up += stage_bytes(sg, twin);
                 cur = stage_after<true>(cur, sg);
             }
             for (int cur = sweep_first<false>(N); !sweep_done<false>(cur, N);) {
-                const Stage sg = stage_at<false>(cur, N, rg);
+                const Stage sg = stage_at<false, kBig>(cur, N, rg);
                 per_dn += stage_bytes(sg, twin);
                 cur = stage_after<false>(cur, sg);
             }
@@ -735,15 +766,15 @@ __global__ void __launch_bounds__(32 * kMaxBlockWarps)
             const bool act = pass < t_lane;
             int used;
             if (twin)
-                used = (pass & 1) ? sweep<true, kHalf, true>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act, ht,
-                                                             &tile_counter[1])
-                                  : sweep<false, kHalf, true>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act, ht,
-                                                              &tile_counter[1]);
+                used = (pass & 1) ? sweep<true, kHalf, true, kBig>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act,
+                                                                   ht, &tile_counter[1])
+                                  : sweep<false, kHalf, true, kBig>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act,
+                                                                    ht, &tile_counter[1]);
             else
-                used = (pass & 1) ? sweep<true, kHalf, false>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act, ht,
-                                                              &tile_counter[1])
-                                  : sweep<false, kHalf, false>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act, ht,
-                                                               &tile_counter[1]);
+                used = (pass & 1) ? sweep<true, kHalf, false, kBig>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act,
+                                                                    ht, &tile_counter[1])
+                                  : sweep<false, kHalf, false, kBig>(ring, q, tv, lane, N, rg, cst, sh.c, amer, act,
+                                                                     ht, &tile_counter[1]);
             if (used < 0) return;
             q += (uint32_t)used;
         }
@@ -803,7 +834,9 @@ constexpr int kMaxDevices = 64;
 struct DeviceFacts {
     int sms = 0;
     int l2 = 0;  // L2 bytes
-    int max_blocks[kMaxBlockWarps + 1] = {};  // FP64 streaming solver: blocks per SM by block size
+    // FP64 streaming solver: resident blocks per SM by block size, small and big stages
+    int max_blocks[kMaxBlockWarps + 1] = {};
+    int max_blocks_big[kMaxBlockWarps + 1] = {};
 };
 DeviceFacts g_facts[kMaxDevices];
 std::atomic<bool> g_ready[kMaxDevices];
@@ -821,20 +854,37 @@ void fd1d_prepare_kernels(int device)
     DeviceFacts& f = g_facts[device];
     cudaDeviceGetAttribute(&f.sms, cudaDevAttrMultiProcessorCount, device);
     cudaDeviceGetAttribute(&f.l2, cudaDevAttrL2CacheSize, device);
-    cudaFuncSetAttribute(fd1d_solve_fp64<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(kMaxBlockWarps * kSolveSmem));
-    cudaFuncSetAttribute(fd1d_solve_fp64<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(kMaxBlockWarps * kSolveSmem));
+    constexpr size_t kSmall = Geo<false>::kSolveSmem, kBigSmem = Geo<true>::kSolveSmem;
+    cudaFuncSetAttribute(fd1d_solve_fp64<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(kMaxBlockWarps * kSmall));
+    cudaFuncSetAttribute(fd1d_solve_fp64<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(kMaxBlockWarps * kSmall));
+    cudaFuncSetAttribute(fd1d_solve_fp64<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(kMaxBlockWarps * kBigSmem));
+    cudaFuncSetAttribute(fd1d_solve_fp64<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(kMaxBlockWarps * kBigSmem));
     for (int bw = 1; bw <= kMaxBlockWarps; bw *= 2) {
         int mx = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mx, fd1d_solve_fp64<true>, 32 * bw, bw * kSolveSmem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mx, fd1d_solve_fp64<true, false>, 32 * bw, bw * kSmall);
         f.max_blocks[bw] = mx < 1 ? 1 : mx;
+        mx = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mx, fd1d_solve_fp64<true, true>, 32 * bw, bw * kBigSmem);
+        f.max_blocks_big[bw] = mx;  // 0: does not fit
     }
     fd1d_fp32_prepare(device);
     fd1d_pcr64_prepare(device);
     if (prev >= 0 && prev != device) cudaSetDevice(prev);
     g_ready[device].store(true, std::memory_order_release);
 }
+
+namespace {
+// Big stages when the launch caps the residency (sm_blocks > 0) at a level their
+// shared memory allows: then every resident warp gets the bigger ring.
+bool use_big_stages(const DeviceFacts& f, int bw, int sm_blocks)
+{
+    return sm_blocks > 0 && sm_blocks <= f.max_blocks_big[bw];
+}
+}  // namespace
 
 int fd1d_fp64_solve_blocks(int ntiles, int device, int block_warps, int sm_blocks)
 {
@@ -843,7 +893,9 @@ int fd1d_fp64_solve_blocks(int ntiles, int device, int block_warps, int sm_block
     const DeviceFacts& f = g_facts[device];
     const int bw = block_warps == 2 || block_warps == 4 ? block_warps : 1;
     const int want = (ntiles + bw - 1) / bw;  // one tile per warp at most
-    const int per_sm = sm_blocks > 0 && sm_blocks < f.max_blocks[bw] ? sm_blocks : f.max_blocks[bw];
+    const int per_sm = use_big_stages(f, bw, sm_blocks) ? sm_blocks
+                       : sm_blocks > 0 && sm_blocks < f.max_blocks[bw] ? sm_blocks
+                                                                       : f.max_blocks[bw];
     const int cap = (f.sms > 0 ? f.sms : 1) * per_sm;
     return want < cap ? (want > 0 ? want : 1) : cap;
 }
@@ -868,19 +920,30 @@ int fd1d_fp64_launch(const PdeBatch& b, const AssetBatch& a, const Fd1dShape& sh
     cudaMemsetAsync(counters, 0, 4 * sizeof(int), stream);
     if (ev) cudaEventRecord(ev->start, stream);
     const int bw = sh.block_warps == 2 || sh.block_warps == 4 ? sh.block_warps : 1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const bool known = dev >= 0 && dev < kMaxDevices;
     {
         // nodes per sweep end kept in L2: a share of the L2 split over the resident warps
         // (each node is 32 lanes x 16 B of state)
-        int dev = 0;
-        cudaGetDevice(&dev);
-        const long long l2 = dev >= 0 && dev < kMaxDevices ? g_facts[dev].l2 : 0;
+        const long long l2 = known ? g_facts[dev].l2 : 0;
         const long long warps = (long long)solve_blocks * bw;
         sh.keep_nodes = warps > 0 ? (int)((long long)(kKeepShare * (double)l2) / (warps * kTile * 16)) : 0;
     }
-    if (sh.c == 1.)
-        fd1d_solve_fp64<true><<<solve_blocks, 32 * bw, bw * kSolveSmem, stream>>>(b, sh, work, counters);
-    else
-        fd1d_solve_fp64<false><<<solve_blocks, 32 * bw, bw * kSolveSmem, stream>>>(b, sh, work, counters);
+    // the same choice fd1d_fp64_solve_blocks made for the grid size
+    const bool big = known && use_big_stages(g_facts[dev], bw, sh.sm_blocks);
+    const size_t smem = bw * (big ? Geo<true>::kSolveSmem : Geo<false>::kSolveSmem);
+    if (sh.c == 1.) {
+        if (big)
+            fd1d_solve_fp64<true, true><<<solve_blocks, 32 * bw, smem, stream>>>(b, sh, work, counters);
+        else
+            fd1d_solve_fp64<true, false><<<solve_blocks, 32 * bw, smem, stream>>>(b, sh, work, counters);
+    } else {
+        if (big)
+            fd1d_solve_fp64<false, true><<<solve_blocks, 32 * bw, smem, stream>>>(b, sh, work, counters);
+        else
+            fd1d_solve_fp64<false, false><<<solve_blocks, 32 * bw, smem, stream>>>(b, sh, work, counters);
+    }
     if (ev) {
         cudaEventRecord(ev->stop, stream);
         if (ev->bytes) cudaMemcpyAsync(ev->bytes, counters + 2, sizeof(unsigned long long), cudaMemcpyDeviceToHost,

@@ -453,6 +453,34 @@ def test_streaming_solver_repeats_bit_for_bit(ctx):
     assert rc == 0 and rel_err(host[idx], want) <= REL_TOL
 
 
+@pytest.mark.parametrize("grid", [dict(x_dim=1024, t_dim=64, density=math.inf),
+                                  dict(x_dim=512, t_dim=48, density=0.25),
+                                  dict(x_dim=2048, t_dim=16, density=math.inf),
+                                  dict(x_dim=13, t_dim=9, density=math.inf)],
+                         ids=["uniform1024", "sinh512", "uniform2048", "uniform13"])
+def test_stage_geometries_agree_bit_for_bit(ctx, grid):
+    """The streaming solver's big stages (16-node coefficient stages, 32-node middle
+    stages, taken when the launch caps the residency: 4-warp blocks one per SM, 2-warp
+    blocks two per SM, 1-warp blocks four per SM) give the same bits as the small
+    stages of a full-residency launch, for FD1D and for FD1D-BS twin tiles.  On the
+    13-node grid every big-stage sweep is a single tail stage."""
+    import kwg
+    import portfolio
+
+    o = portfolio.american_portfolio(2048, seed=77)
+    o["e"][::5] = 0  # some European options: mixed classes, and twin tiles for FD1D-BS
+    common = dict(scale=5.0, solver=kwg.SOLVER_THOMAS, **grid)
+    want, st = gpu_price(ctx, o, block_warps=1, sm_blocks=0, **common)
+    assert (st == 0).all()
+    for bw, sb in ((4, 1), (2, 2), (1, 4)):
+        got, st = gpu_price(ctx, o, block_warps=bw, sm_blocks=sb, **common)
+        assert (st == 0).all() and np.array_equal(got, want), (bw, sb, int((got != want).sum()))
+    rc, bs_small, st = ctx.fd1d_bs_price(o, kwg.params(block_warps=1, sm_blocks=0, **common))
+    assert rc == 0 and (st == 0).all()
+    rc, bs_big, st = ctx.fd1d_bs_price(o, kwg.params(block_warps=4, sm_blocks=1, **common))
+    assert rc == 0 and (st == 0).all() and np.array_equal(bs_big, bs_small)
+
+
 def test_solvers_agree_and_autotune(ctx):
     """Both FP64 solvers give the same prices to 1e-10; the autotuner times both and
     AUTO then matches them too."""
