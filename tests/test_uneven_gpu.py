@@ -36,6 +36,25 @@ def sample(n, seed=42):
     return o[idx], xd[idx], td[idx]
 
 
+def test_uneven_big_stages_match_small_stages(ctx):
+    """One 4-warp block per SM (the tuned shape of uneven batches) runs the streaming
+    solver's big stages; a full-residency launch runs the small ones.  Tiles of every
+    node count from 128 to 2048, each lane with its own step count: the same bits."""
+    import kwg
+
+    o, xd, td = sample(4096, seed=3)
+    td = np.minimum(td, 160)
+    rc, small, st = ctx.fd1d_price_uneven(o, xd, td, kwg.params(scale=SCALE, density=math.inf, solver=1,
+                                                                  block_warps=1, sm_blocks=0))
+    assert rc == 0, ctx.last_error()
+    rc, big, st2 = ctx.fd1d_price_uneven(o, xd, td, kwg.params(scale=SCALE, density=math.inf, solver=1,
+                                                                 block_warps=4, sm_blocks=1))
+    assert rc == 0, ctx.last_error()
+    assert np.array_equal(st, st2) and (st == 0).sum() > 0.8 * len(o)
+    ok = st == 0
+    assert np.array_equal(big[ok], small[ok])
+
+
 @pytest.mark.parametrize("solver", [1, 2], ids=["thomas", "pcr"])
 def test_uneven_fp64_matches_oracle_per_shape(ctx, solver):
     import kwg
