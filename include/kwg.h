@@ -36,7 +36,8 @@ extern "C" {
 /* ---- per-option status (status[i]) --------------------------------------------------- */
 #define KWG_STATUS_OK 0
 #define KWG_STATUS_OUT_OF_GRID 1 /* price is NaN; the reference fails the whole batch here */
-#define KWG_STATUS_SOLVER 2      /* price is NaN; zero/non-finite pivot in the factorisation */
+#define KWG_STATUS_SOLVER 2      /* price is NaN; zero/non-finite pivot in the factorisation, or a non-finite
+                                    value where the price is read (FP32: values beyond its range) */
 #define KWG_STATUS_BAD_INPUT 3   /* price is NaN; t<=0, z<=0, k<=0 or s<=0 */
 #define KWG_STATUS_DEVICE_TIMEOUT 4 /* price is NaN; a bounded device-side wait expired */
 

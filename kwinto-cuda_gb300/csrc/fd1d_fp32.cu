@@ -753,6 +753,12 @@ __global__ void fd1d_interp_rows(const PdeBatch b, const AssetBatch a, Fd1dShape
             price = mul(k, v);
         }
     }
+    // a solve that left a non-finite value where the price is read is a solver failure
+    // (the FP32 path's float-float state overflows beyond ~3.4e38 x K)
+    if (st == KWG_STATUS_OK && !isfinite(price)) {
+        st = KWG_STATUS_SOLVER;
+        price = __longlong_as_double(0x7ff8000000000000ll);
+    }
     prices[i] = price;
     if (status) status[i] = st;
 }

@@ -27,9 +27,11 @@
 // the reference does ~40 plus 5 divisions.  max() runs on the integer pipe.
 //
 // Uniform grids (density = +inf).  Rows come from the exact spacing h, so interior
-// rows are identical; the pivot recurrences d_j, e_j then converge and are frozen at
-// their limit (a change of an ulp or two).  Nodes whose six coefficients are all
-// frozen form a middle region where a sweep streams only (p, V, state).
+// rows are identical; the pivot recurrences d_j, e_j then converge, and once a step
+// reproduces its input bit for bit (a fixed point of the rounded recurrence) every
+// later pivot equals it: the pivot is frozen with no approximation.  Nodes whose six
+// coefficients are all frozen form a middle region where a sweep streams only
+// (p, V, state).
 //
 // Layout (option-interleaved, one tile = 32 PDEs = one warp, lane = PDE), arrays per
 // tile and node so that a run of consecutive nodes is contiguous for each sweep:
@@ -122,10 +124,6 @@ __device__ __forceinline__ TileView tile_view(const Work& w, long long off)
     return v;
 }
 
-// The pivot recurrences are frozen once a step changes them by at most this
-// relative amount (uniform grids only, where the interior rows are identical).
-constexpr double kFreeze = 0x1p-50;
-
 }  // namespace
 
 namespace {
@@ -179,7 +177,8 @@ __device__ __forceinline__ void setup_slot(const PdeBatch& b, const Fd1dShape& s
                 d = d_prev;
             } else {
                 d = sub(tm, mul(dvd(tl, d_prev), tu_prev));
-                if (sh.uniform && j >= 3 && j < N - 1 && fabs(d - d_prev) <= kFreeze * fabs(d)) {
+                // a fixed point: with identical interior rows every later d_j equals it
+                if (sh.uniform && j >= 3 && j < N - 1 && d == d_prev) {
                     lu_frozen = true;
                     lu_freeze = j;
                     d = d_prev;
@@ -210,7 +209,7 @@ __device__ __forceinline__ void setup_slot(const PdeBatch& b, const Fd1dShape& s
                 e = e_next;
             } else {
                 e = sub(tm, mul(m, tl_next));
-                if (sh.uniform && j <= N - 4 && j > 0 && fabs(e - e_next) <= kFreeze * fabs(e)) {
+                if (sh.uniform && j <= N - 4 && j > 0 && e == e_next) {
                     ul_frozen = true;
                     ul_freeze = j;
                     e = e_next;
@@ -822,6 +821,11 @@ __global__ void fd1d_interp_fp64(const PdeBatch b, const AssetBatch a, Fd1dShape
             const double v = dvd(add(mul(sub(xh, xs), vl), mul(sub(xs, xl), vh)), sub(xh, xl));
             price = mul(k, v);
         }
+    }
+    // a solve that left a non-finite value where the price is read is a solver failure
+    if (st == KWG_STATUS_OK && !isfinite(price)) {
+        st = KWG_STATUS_SOLVER;
+        price = __longlong_as_double(0x7ff8000000000000ll);
     }
     prices[i] = price;
     if (status) status[i] = st;

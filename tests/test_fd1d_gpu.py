@@ -544,3 +544,62 @@ def test_single_option(ctx, entry):
         p, st = d_p.cpu().numpy(), d_s.cpu().numpy()
     assert rc == 0 and st[0] == 0
     assert rel_err(p, want) <= REL_TOL
+
+
+def extreme_sweep():
+    """1296 options over the corners of the parameter space: spot 50/100/200 against
+    strike 100, vol 2 %..150 %, maturity 0.01..5 years, r and q 0..20 %, American and
+    European puts and calls.  A third of them fall outside the grid."""
+    import itertools
+
+    import kwg
+
+    rows = [(t, 100.0, z, r, q, s, e, w)
+            for s, z, t, r, q, e, w in itertools.product((50.0, 100.0, 200.0), (0.02, 0.1, 0.6, 1.5),
+                                                         (0.01, 0.5, 5.0), (0.0, 0.05, 0.2), (0.0, 0.03, 0.2),
+                                                         (0, 1), (-1, 1))]
+    return np.array(rows, dtype=kwg.OPTION_DTYPE)
+
+
+@pytest.mark.parametrize("grid", [dict(x_dim=256, t_dim=128, scale=5.0, density=math.inf),
+                                  dict(x_dim=256, t_dim=128, scale=5.0, density=0.25),
+                                  dict(x_dim=1024, t_dim=64, scale=5.0, density=math.inf),
+                                  dict(x_dim=300, t_dim=50, scale=50.0, density=0.25)],
+                         ids=["uniform256", "sinh256", "uniform1024x64", "sinh300_scale50"])
+def test_extreme_parameters_match_the_oracle(ctx, grid):
+    """FD1D and FD1D-BS on the extreme sweep, both FP64 solvers: the out-of-grid
+    options flagged as the oracle flags them, every other price within REL_TOL of the
+    oracle (prices below 1e-6 K within 1e-13 K absolute: they reach 1e-29).  The FP32
+    path reports every price it cannot represent with a status, never as a NaN with
+    status OK (at scale 50 a call's grid reaches e^168 K, beyond FP32's range).  The
+    pivots freeze only at an exact fixed point: with the earlier 2^-50 tolerance the
+    drift-dominated options (vol 2 %, |r - q| = 0.2, T = 5) missed REL_TOL at 1024 x 64."""
+    import kwg
+    import kwor
+
+    o = extreme_sweep()
+    rc, msg, want, wst = kwor.fd1d_price(o, **grid)
+    ok = wst == 0
+    assert 0.5 * len(o) < ok.sum() < len(o)
+    v = o[ok]
+    rc, msg, want_bs, _ = kwor.fd1d_price(v, bs=True, **grid)  # the reference fails a batch with an out-of-grid option
+    assert rc == 0, msg
+
+    def check(got, ref):
+        k = v["k"]
+        big = np.abs(ref) >= 1e-6 * k
+        assert rel_err(got[big], ref[big]) <= REL_TOL
+        assert np.max(np.abs(got[~big] - ref[~big]) / k[~big], initial=0.0) <= 1e-13
+
+    for solver in (kwg.SOLVER_THOMAS, kwg.SOLVER_PCR):
+        prm = kwg.params(solver=solver, **grid)
+        p, st = gpu_price(ctx, o, solver=solver, **grid)
+        assert np.array_equal(st == kwg.STATUS_OUT_OF_GRID, wst == 1) and (st[ok] == 0).all()
+        check(p[ok], want[ok])
+        rc, p_bs, st_bs = ctx.fd1d_bs_price(v, prm)
+        assert rc == 0 and (st_bs == 0).all()
+        check(p_bs, want_bs)
+    p32, st32 = gpu_price(ctx, o, precision=kwg.FP32, **grid)
+    assert np.isfinite(p32[st32 == 0]).all()
+    assert np.isnan(p32[st32 != 0]).all()
+    assert np.array_equal(st32 == kwg.STATUS_OUT_OF_GRID, wst == 1)
