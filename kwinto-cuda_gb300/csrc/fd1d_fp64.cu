@@ -128,9 +128,33 @@ __device__ __forceinline__ TileView tile_view(const Work& w, long long off)
 
 namespace {
 
+// A correctly rounded division with a one-entry cache: on a uniform grid the frozen
+// middle region divides the same operands (by their bits) at every node, and the
+// cache returns the quotient the division gave the first time -- the same bits.
+struct DivMemo {
+    long long x = 0, y = 0;
+    double q = 0.;
+    bool valid = false;
+    __device__ __forceinline__ double operator()(double a, double b)
+    {
+        const long long xa = __double_as_longlong(a), yb = __double_as_longlong(b);
+        if (!valid || xa != x || yb != y) {
+            x = xa;
+            y = yb;
+            q = dvd(a, b);
+            valid = true;
+        }
+        return q;
+    }
+};
+
 // The setup of one PDE slot.  cw, cl: the width of the tile's coefficient and payoff
 // records and this slot's index in them -- kTile and the lane, or in twin tiles 16 and
 // lane / 2 (one record per twin pair).
+// It is FP64-pipe bound (divisions, the payoff's exp).  On a uniform grid it computes
+// the interior row once, divides through one-entry caches and skips exp where the
+// payoff is +0 (x >= 0 for a put, x <= 0 for a call: 1 - e^x <= 0, e^x - 1 <= 0), all
+// bit-identical to evaluating every node.
 __device__ __forceinline__ void setup_slot(const PdeBatch& b, const Fd1dShape& sh, const Work& wk, const TileView& tv,
                                            int slot, int src, int lane, int N, int cw, int cl,
                                            int32_t* __restrict__ pde_status)
@@ -161,33 +185,48 @@ __device__ __forceinline__ void setup_slot(const PdeBatch& b, const Fd1dShape& s
     double d_prev = 1., tu_prev = 0.;
     bool lu_frozen = false;
     int lu_freeze = N;  // first j whose d_j was frozen
+    Row t_int;          // uniform grids: theta x the interior row (the same at every interior node)
+    bool have_int = false;
+    DivMemo div_l;      // tl / d_prev
     for (int j = 0; j < N; ++j) {
         if (j > 0) {
             xm = x0;
             x0 = xp;
             xp = (j + 1 < N) ? g.x(j + 1) : 0.;
         }
-        const Row r = sh.uniform ? implicit_row(j, N, -hx, 0., hx, theta, dt, a.a0, a.ax, a.axx)
-                                 : implicit_row(j, N, xm, x0, xp, theta, dt, a.a0, a.ax, a.axx);
-        const double tl = mul(theta, r.bl), tm = mul(theta, r.b), tu = mul(theta, r.bu);
-        const double p = payoff(w, x0);
+        auto scaled = [&](const Row& r) { return Row{mul(theta, r.bl), mul(theta, r.b), mul(theta, r.bu)}; };
+        Row tr;
+        if (!sh.uniform) {
+            tr = scaled(implicit_row(j, N, xm, x0, xp, theta, dt, a.a0, a.ax, a.axx));
+        } else if (j == 0 || j == N - 1) {
+            tr = scaled(implicit_row(j, N, -hx, 0., hx, theta, dt, a.a0, a.ax, a.axx));
+        } else {
+            if (!have_int) t_int = scaled(implicit_row(j, N, -hx, 0., hx, theta, dt, a.a0, a.ax, a.axx));
+            have_int = true;
+            tr = t_int;
+        }
+        const double tl = tr.bl, tm = tr.b, tu = tr.bu;
+        const double p = ((w < 0) ? (x0 < 0.) : (x0 > 0.)) ? payoff(w, x0) : 0.;
+        const double l = j > 0 ? div_l(tl, d_prev) : 0.;
         double d = tm;
         if (j > 0) {
             if (lu_frozen && j < N - 1) {
-                d = d_prev;
+                d = d_prev;  // checked when it was computed
             } else {
-                d = sub(tm, mul(dvd(tl, d_prev), tu_prev));
+                d = sub(tm, mul(l, tu_prev));
                 // a fixed point: with identical interior rows every later d_j equals it
                 if (sh.uniform && j >= 3 && j < N - 1 && d == d_prev) {
                     lu_frozen = true;
                     lu_freeze = j;
                     d = d_prev;
                 }
+                if (!finite_nonzero(d) && st == KWG_STATUS_OK) st = KWG_STATUS_SOLVER;
             }
+        } else if (!finite_nonzero(d) && st == KWG_STATUS_OK) {
+            st = KWG_STATUS_SOLVER;
         }
-        if (!finite_nonzero(d) && st == KWG_STATUS_OK) st = KWG_STATUS_SOLVER;
         CU(j, 0) = tl;  // parked
-        CU(j, 1) = j > 0 ? dvd(tl, d_prev) : 0.;
+        CU(j, 1) = l;
         P(j) = p;
         S(j, 0) = p;
         CD(j, 0) = d;   // parked
@@ -200,13 +239,16 @@ __device__ __forceinline__ void setup_slot(const PdeBatch& b, const Fd1dShape& s
     double e_next = 1., tl_next = 0., h_next = 0., d_next = 1.;
     bool ul_frozen = false;
     int ul_freeze = -1;  // first j (from the top) whose e_j was frozen
+    DivMemo div_m, div_nh, div_ie, div_uh, div_id;
     for (int j = N - 1; j >= 0; --j) {
         const double tl = CU(j, 0), d = CD(j, 0), tu = CD(j, 1), tm = CD(j, 2);
         double e = tm, m = 0.;
+        bool fresh = true;  // e computed here (not the frozen value, checked before)
         if (j < N - 1) {
-            m = dvd(tu, e_next);
+            m = div_m(tu, e_next);
             if (ul_frozen && j > 0) {
                 e = e_next;
+                fresh = false;
             } else {
                 e = sub(tm, mul(m, tl_next));
                 if (sh.uniform && j <= N - 4 && j > 0 && e == e_next) {
@@ -216,13 +258,13 @@ __device__ __forceinline__ void setup_slot(const PdeBatch& b, const Fd1dShape& s
                 }
             }
         }
-        if (!finite_nonzero(e) && st == KWG_STATUS_OK) st = KWG_STATUS_SOLVER;
+        if (fresh && !finite_nonzero(e) && st == KWG_STATUS_OK) st = KWG_STATUS_SOLVER;
         // row j+1's nh = Tl_{j+1} / e_j, written now that e_j is known
-        if (j < N - 1) CU(j + 1, 0) = dvd(tl_next, e);
-        CU(j, 2) = dvd(1., e);
-        CD(j, 0) = j < N - 1 ? dvd(tu, d_next) : 0.;
+        if (j < N - 1) CU(j + 1, 0) = div_nh(tl_next, e);
+        CU(j, 2) = div_ie(1., e);
+        CD(j, 0) = j < N - 1 ? div_uh(tu, d_next) : 0.;
         CD(j, 1) = m;
-        CD(j, 2) = dvd(1., d);
+        CD(j, 2) = div_id(1., d);
         const double h = fma(-m, h_next, P(j));
         S(j, 1) = h;
         e_next = e;
