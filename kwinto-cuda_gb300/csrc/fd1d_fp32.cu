@@ -262,11 +262,12 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
         // uniform grids: operator rows from the exact spacing, as the FP64 solvers build
         // them; the interior row is the same at every interior node, so it is built once
         // (three divisions per node fewer in this FP64 prologue)
-        const double hxu = sh.uniform ? dvd(sub(g.xMax, g.xMin), (double)(N - 1)) : 0.;
+        const bool uni = kUni || sh.uniform;  // kUni: a uniform grid of full lanes
+        const double hxu = uni ? dvd(sub(g.xMax, g.xMin), (double)(N - 1)) : 0.;
         Row row_int{};
         bool have_int = false;
         auto row_at = [&](int j, double xm, double x0, double xp) -> Row {
-            if (!sh.uniform) return implicit_row(j, N, xm, x0, xp, sh.theta, dt, a.a0, a.ax, a.axx);
+            if (!uni) return implicit_row(j, N, xm, x0, xp, sh.theta, dt, a.a0, a.ax, a.axx);
             if (j == 0 || j == N - 1) return implicit_row(j, N, -hxu, 0., hxu, sh.theta, dt, a.a0, a.ax, a.axx);
             if (!have_int) row_int = implicit_row(j, N, -hxu, 0., hxu, sh.theta, dt, a.a0, a.ax, a.axx);
             have_int = true;
@@ -280,6 +281,13 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
         {
             double xm = (j0 > 0 && j0 - 1 < N) ? g.x(j0 - 1) : 0.;
             double x0 = (j0 < N) ? g.x(j0) : 0.;
+            // uniform grids: e^x of the lane's nodes by one exp and a product per node
+            // (the payoff needs ~1e-15 here, the float-float state's precision)
+            double ex = 1., ex_step = 1.;
+            if (uni && j0 < N) {
+                ex = exp(x0);
+                ex_step = exp(hxu);
+            }
             double d_prev = 1., id_prev = 1., bu_prev = 0.;
             double pu = 1., pl = 1., sum = 0., fL = 0., bl_first = 0., pr = 1.;
 #pragma unroll 1
@@ -306,8 +314,14 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
                         c2 = (float)(dt * (a.axx * (u2 - l2) + a.ax * im));
                         c3 = (float)(dt * a.ax * im);
                     }
-                    // the payoff is exactly 0 on the out-of-the-money side: skip exp there
-                    if ((w < 0) ? (x0 < 0.) : (x0 > 0.)) p = split(payoff(w, x0));
+                    if (uni) {
+                        const double v = (w < 0) ? 1. - ex : ex - 1.;
+                        if (v > 0.) p = split(v);
+                        ex *= ex_step;
+                    } else if ((w < 0) ? (x0 < 0.) : (x0 > 0.)) {
+                        // the payoff is exactly 0 on the out-of-the-money side: skip exp there
+                        p = split(payoff(w, x0));
+                    }
                 }
                 if (!kUni) set_c(i, c1, c2, c3, c4);
                 PH(i) = p.hi;
