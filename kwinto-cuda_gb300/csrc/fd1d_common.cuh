@@ -65,42 +65,50 @@ __device__ __forceinline__ double payoff(int8_t w, double x)
     return (0. < v) ? v : 0.;
 }
 
-// Row j of the reference's implicit matrix B = 1 - theta dt A
-// (src/Math/kwFd1d.cpp:73-114), with the reference's operation order; returns
-// (bl, b, bu).  xm, x0, xp are x_{j-1}, x_j, x_{j+1} (unused ones ignored).
+// One row (bl, b, bu) of a tridiagonal matrix.
 struct Row {
     double bl, b, bu;
 };
 
-__device__ __forceinline__ Row implicit_row(int j, int n, double xm, double x0, double xp,
-                                            double theta, double dt, double a0, double ax,
-                                            double axx)
+// Row j of the reference's implicit matrix B = 1 - theta dt A
+// (src/Math/kwFd1d.cpp:73-114), with the reference's operation order, from the
+// reciprocal spacings inv_u = 1/(xp - x0), inv_m = 1/(xp - xm),
+// inv_d = 1/(x0 - xm) (row 0 reads inv_u, row n-1 inv_d): a caller walking the grid
+// passes a node's inv_u on as the next node's inv_d.  Bit-identical to implicit_row.
+__device__ __forceinline__ Row implicit_row_r(int j, int n, double inv_u, double inv_m, double inv_d,
+                                              double theta, double dt, double a0, double ax, double axx)
 {
     Row r;
     const double tdt = mul(theta, dt);    // theta * dt
     const double ntdt = mul(-theta, dt);  // -theta * dt
     if (j == 0) {
-        const double inv_dx = dvd(1., sub(xp, x0));
         r.bl = 0.;
-        r.b = sub(1., mul(tdt, sub(a0, mul(inv_dx, ax))));
-        r.bu = mul(ntdt, mul(inv_dx, ax));
+        r.b = sub(1., mul(tdt, sub(a0, mul(inv_u, ax))));
+        r.bu = mul(ntdt, mul(inv_u, ax));
     } else if (j == n - 1) {
-        const double inv_dx = dvd(1., sub(x0, xm));
-        r.bl = mul(ntdt, mul(-inv_dx, ax));
-        r.b = sub(1., mul(tdt, add(a0, mul(inv_dx, ax))));
+        r.bl = mul(ntdt, mul(-inv_d, ax));
+        r.b = sub(1., mul(tdt, add(a0, mul(inv_d, ax))));
         r.bu = 0.;
     } else {
-        const double inv_dxu = dvd(1., sub(xp, x0));
-        const double inv_dxm = dvd(1., sub(xp, xm));
-        const double inv_dxd = dvd(1., sub(x0, xm));
-        const double inv_dx2u = mul(mul(2., inv_dxu), inv_dxm);
-        const double inv_dx2m = mul(mul(2., inv_dxd), inv_dxu);
-        const double inv_dx2l = mul(mul(2., inv_dxd), inv_dxm);
-        r.bl = mul(ntdt, add(mul(-inv_dxm, ax), mul(inv_dx2l, axx)));
+        const double inv_dx2u = mul(mul(2., inv_u), inv_m);
+        const double inv_dx2m = mul(mul(2., inv_d), inv_u);
+        const double inv_dx2l = mul(mul(2., inv_d), inv_m);
+        r.bl = mul(ntdt, add(mul(-inv_m, ax), mul(inv_dx2l, axx)));
         r.b = sub(1., mul(tdt, sub(a0, mul(inv_dx2m, axx))));
-        r.bu = mul(ntdt, add(mul(inv_dxm, ax), mul(inv_dx2u, axx)));
+        r.bu = mul(ntdt, add(mul(inv_m, ax), mul(inv_dx2u, axx)));
     }
     return r;
+}
+
+// The same row from the nodes: xm, x0, xp are x_{j-1}, x_j, x_{j+1} (unused ones ignored).
+__device__ __forceinline__ Row implicit_row(int j, int n, double xm, double x0, double xp,
+                                            double theta, double dt, double a0, double ax,
+                                            double axx)
+{
+    if (j == 0) return implicit_row_r(j, n, dvd(1., sub(xp, x0)), 0., 0., theta, dt, a0, ax, axx);
+    if (j == n - 1) return implicit_row_r(j, n, 0., 0., dvd(1., sub(x0, xm)), theta, dt, a0, ax, axx);
+    return implicit_row_r(j, n, dvd(1., sub(xp, x0)), dvd(1., sub(xp, xm)), dvd(1., sub(x0, xm)), theta, dt, a0,
+                          ax, axx);
 }
 
 // PDE coefficients of one option (src/Pricer/kwFd1d.cpp:79-85):

@@ -266,8 +266,11 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
         const double hxu = uni ? dvd(sub(g.xMax, g.xMin), (double)(N - 1)) : 0.;
         Row row_int{};
         bool have_int = false;
-        auto row_at = [&](int j, double xm, double x0, double xp) -> Row {
-            if (!uni) return implicit_row(j, N, xm, x0, xp, sh.theta, dt, a.a0, a.ax, a.axx);
+        // other grids: rows from the reciprocal spacings the loops below carry from node
+        // to node (two divisions per node instead of three for the row and three for
+        // the residual coefficients)
+        auto row_at = [&](int j, double iu, double im, double id) -> Row {
+            if (!uni) return implicit_row_r(j, N, iu, im, id, sh.theta, dt, a.a0, a.ax, a.axx);
             if (j == 0 || j == N - 1) return implicit_row(j, N, -hxu, 0., hxu, sh.theta, dt, a.a0, a.ax, a.axx);
             if (!have_int) row_int = implicit_row(j, N, -hxu, 0., hxu, sh.theta, dt, a.a0, a.ax, a.axx);
             have_int = true;
@@ -290,6 +293,8 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
             }
             double d_prev = 1., id_prev = 1., bu_prev = 0.;
             double pu = 1., pl = 1., sum = 0., fL = 0., bl_first = 0., pr = 1.;
+            // 1 / (x_j - x_{j-1}) of the current node (the previous node's upward reciprocal)
+            double r_d = (!kUni && j0 > 0 && j0 < N) ? 1. / (x0 - xm) : 0.;
 #pragma unroll 1
             for (int i = 0; i < M; ++i) {
                 const int j = j0 + i;
@@ -297,8 +302,14 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
                 double bl = 0., bb = 1., bu = 0.;
                 float c1 = 0.f, c2 = 0.f, c3 = 0.f, c4 = 0.f;
                 FF p = {0.f, 0.f};
+                double r_u = 0.;
                 if (j < N) {
-                    const Row rw = row_at(j, xm, x0, xp);
+                    double r_m = 0.;
+                    if (!kUni) {
+                        if (j + 1 < N) r_u = 1. / (xp - x0);
+                        if (j > 0 && j + 1 < N) r_m = 1. / (xp - xm);
+                    }
+                    const Row rw = row_at(j, r_u, r_m, r_d);
                     bl = rw.bl;
                     bb = rw.b;
                     bu = rw.bu;
@@ -308,7 +319,7 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
                     } else if (j == N - 1) {
                         c3 = (float)(dt * a.ax / (x0 - xm));
                     } else {
-                        const double iu = 1. / (xp - x0), im = 1. / (xp - xm), id = 1. / (x0 - xm);
+                        const double iu = r_u, im = r_m, id = r_d;
                         const double u2 = 2. * iu * im, l2 = 2. * id * im;
                         c1 = (float)(dt * a.axx * l2);
                         c2 = (float)(dt * (a.axx * (u2 - l2) + a.ax * im));
@@ -372,6 +383,7 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
                 bu_prev = bu;
                 xm = x0;
                 x0 = xp;
+                r_d = r_u;
             }
             (void)d_prev;
             L1 = bl_first * sum;
@@ -386,13 +398,21 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
             double e_next = 1., bl_next = 0.;
             const int jt = j0 + M - 1;
             double xp = (jt + 1 < N) ? g.x(jt + 1) : 0., x0 = (jt < N) ? g.x(jt) : 0.;
+            // 1 / (x_{j+1} - x_j) of the current node (the node above's downward reciprocal)
+            double r_u = (!uni && jt + 1 < N) ? 1. / (xp - x0) : 0.;
 #pragma unroll 1
             for (int i = M - 1; i > P; --i) {
                 const int j = j0 + i;
                 const double xm = (j - 1 < N) ? g.x(j - 1) : 0.;
                 double bl = 0., bb = 1., bu = 0.;
+                double r_d = 0.;
                 if (j < N) {
-                    const Row rw = row_at(j, xm, x0, xp);
+                    double r_m = 0.;
+                    if (!uni && j > 0) {
+                        r_d = 1. / (x0 - xm);
+                        if (j + 1 < N) r_m = 1. / (xp - xm);
+                    }
+                    const Row rw = row_at(j, r_u, r_m, r_d);
                     bl = rw.bl;
                     bb = rw.b;
                     bu = rw.bu;
@@ -408,6 +428,7 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
                 bl_next = bl;
                 xp = x0;
                 x0 = xm;
+                r_u = r_d;
             }
             const double m_piv = (P == M - 1) ? 0. : bu_piv / e_next;
             const double gam = b_piv - l_piv * bu_above - m_piv * bl_next;

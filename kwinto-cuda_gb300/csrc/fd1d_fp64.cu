@@ -152,8 +152,9 @@ struct DivMemo {
 // records and this slot's index in them -- kTile and the lane, or in twin tiles 16 and
 // lane / 2 (one record per twin pair).
 // It is FP64-pipe bound (divisions, the payoff's exp).  On a uniform grid it computes
-// the interior row once, divides through one-entry caches and skips exp where the
-// payoff is +0 (x >= 0 for a put, x <= 0 for a call: 1 - e^x <= 0, e^x - 1 <= 0), all
+// the interior row once and divides through one-entry caches; on other grids it builds
+// the rows from reciprocal spacings carried from node to node; it skips exp where the
+// payoff is +0 (x >= 0 for a put, x <= 0 for a call: 1 - e^x <= 0, e^x - 1 <= 0).  All
 // bit-identical to evaluating every node.
 __device__ __forceinline__ void setup_slot(const PdeBatch& b, const Fd1dShape& sh, const Work& wk, const TileView& tv,
                                            int slot, int src, int lane, int N, int cw, int cl,
@@ -188,6 +189,7 @@ __device__ __forceinline__ void setup_slot(const PdeBatch& b, const Fd1dShape& s
     Row t_int;          // uniform grids: theta x the interior row (the same at every interior node)
     bool have_int = false;
     DivMemo div_l;      // tl / d_prev
+    double r_d = 0.;    // other grids: 1 / (x_j - x_{j-1}), the previous node's 1 / (x_{j+1} - x_j)
     for (int j = 0; j < N; ++j) {
         if (j > 0) {
             xm = x0;
@@ -197,7 +199,10 @@ __device__ __forceinline__ void setup_slot(const PdeBatch& b, const Fd1dShape& s
         auto scaled = [&](const Row& r) { return Row{mul(theta, r.bl), mul(theta, r.b), mul(theta, r.bu)}; };
         Row tr;
         if (!sh.uniform) {
-            tr = scaled(implicit_row(j, N, xm, x0, xp, theta, dt, a.a0, a.ax, a.axx));
+            const double r_u = j + 1 < N ? dvd(1., sub(xp, x0)) : 0.;
+            const double r_m = (j > 0 && j + 1 < N) ? dvd(1., sub(xp, xm)) : 0.;
+            tr = scaled(implicit_row_r(j, N, r_u, r_m, r_d, theta, dt, a.a0, a.ax, a.axx));
+            r_d = r_u;
         } else if (j == 0 || j == N - 1) {
             tr = scaled(implicit_row(j, N, -hx, 0., hx, theta, dt, a.a0, a.ax, a.axx));
         } else {

@@ -94,18 +94,39 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64_pcr(const PdeBatch b, Fd1d
             double xm = (j0 > 0 && j0 - 1 < N) ? g.x(j0 - 1) : 0.;
             double x0 = (j0 < N) ? g.x(j0) : 0.;
             double d_prev = 1., tu_prev = 0.;
+            // Bit-identical shortcuts of this FP64 prologue: on uniform grids theta x the
+            // interior row is built once; elsewhere the row comes from reciprocal spacings
+            // carried from node to node (two divisions per node instead of three); no exp
+            // where the payoff is +0 (x >= 0 for a put, x <= 0 for a call).
+            Row t_int{};
+            bool have_int = false;
+            double r_d = (!sh.uniform && j0 > 0 && j0 < N) ? dvd(1., sub(x0, xm)) : 0.;
 #pragma unroll 1
             for (int i = 0; i < M; ++i) {
                 const int j = j0 + i;
                 const double xp = (j + 1 < N) ? g.x(j + 1) : 0.;
                 double tl = 0., tm = 1., tu = 0., p = 0.;
+                double r_u = 0.;
                 if (j < N) {
-                    const Row r = sh.uniform ? implicit_row(j, N, -hx, 0., hx, sh.theta, dt, a.a0, a.ax, a.axx)
-                                             : implicit_row(j, N, xm, x0, xp, sh.theta, dt, a.a0, a.ax, a.axx);
-                    tl = mul(sh.theta, r.bl);
-                    tm = mul(sh.theta, r.b);
-                    tu = mul(sh.theta, r.bu);
-                    p = payoff(w, x0);
+                    auto scaled = [&](const Row& r) {
+                        return Row{mul(sh.theta, r.bl), mul(sh.theta, r.b), mul(sh.theta, r.bu)};
+                    };
+                    Row tr;
+                    if (!sh.uniform) {
+                        if (j + 1 < N) r_u = dvd(1., sub(xp, x0));
+                        const double r_m = (j > 0 && j + 1 < N) ? dvd(1., sub(xp, xm)) : 0.;
+                        tr = scaled(implicit_row_r(j, N, r_u, r_m, r_d, sh.theta, dt, a.a0, a.ax, a.axx));
+                    } else if (j == 0 || j == N - 1) {
+                        tr = scaled(implicit_row(j, N, -hx, 0., hx, sh.theta, dt, a.a0, a.ax, a.axx));
+                    } else {
+                        if (!have_int) t_int = scaled(implicit_row(j, N, -hx, 0., hx, sh.theta, dt, a.a0, a.ax, a.axx));
+                        have_int = true;
+                        tr = t_int;
+                    }
+                    tl = tr.bl;
+                    tm = tr.b;
+                    tu = tr.bu;
+                    p = ((w < 0) ? (x0 < 0.) : (x0 > 0.)) ? payoff(w, x0) : 0.;
                 }
                 Q(i, Q_P) = p;
                 if (i == 0) {
@@ -129,6 +150,7 @@ __global__ void __launch_bounds__(32) fd1d_solve_fp64_pcr(const PdeBatch b, Fd1d
                 tu_prev = tu;
                 xm = x0;
                 x0 = xp;
+                r_d = r_u;
             }
         }
         // spikes L = T_I^-1 (tl_first e_1), R = T_I^-1 (tu_last e_{M-1})
