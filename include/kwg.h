@@ -274,9 +274,11 @@ int kwg_mlp_featurize(kwg_mlp* h, const kwg_option* d_opts, int n, float* d_x, u
 /* Trains on device options with their FD prices (device): premium targets scaled to
  * unit standard deviation, exercise-region floors, Adam with a cosine learning-rate
  * schedule, shuffled minibatches.  The network keeps the parameters of the epoch with
- * the lowest mean minibatch loss; an epoch whose mean loss is not finite or exceeds
- * 3x that best returns to the best parameters with fresh Adam moments and halves the
- * learning rate for the remaining epochs.  *final_loss = the kept epoch's mean loss. */
+ * the lowest mean minibatch loss (the initial ones until an epoch's loss is finite);
+ * an epoch whose mean loss is not finite or exceeds 3x that best returns to those
+ * parameters with fresh Adam moments and halves the learning rate for the remaining
+ * epochs.  *final_loss = the kept epoch's mean loss (the last epoch's when none was
+ * finite). */
 int kwg_mlp_train(kwg_mlp* h, const kwg_option* d_opts, const double* d_prices, int n, int epochs, int batch,
                   float lr, uint64_t seed, double* final_loss);
 /* The last kwg_mlp_train run of h: copies min(epochs, cap) per-epoch mean losses to

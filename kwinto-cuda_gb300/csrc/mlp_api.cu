@@ -502,15 +502,21 @@ int kwg_mlp_train(kwg_mlp* h, const kwg_option* d_opts, const double* d_prices, 
     const int steps_per_epoch = (n + batch - 1) / batch;
     const long long total = (long long)steps_per_epoch * epochs;
     long long step = 0;
-    // the parameters of the epoch with the lowest mean loss are kept; an epoch whose
-    // loss is not finite or above kSpike x that best goes back to them with fresh Adam
-    // moments and half the learning rate for the rest of the run
+    // the parameters of the epoch with the lowest mean loss are kept (before the first
+    // finite epoch: the initial ones); an epoch whose loss is not finite or above
+    // kSpike x that best goes back to them with fresh Adam moments and half the
+    // learning rate for the rest of the run
     constexpr double kSpike = 3.;
     double best = HUGE_VAL;
     float lr_scale = 1.f;
     h->loss_hist.clear();
     h->best_epoch = -1;
     h->restarts = 0;
+    if (cudaMemcpyAsync(pbest, h->p, sizeof(float) * kMlpParams, cudaMemcpyDeviceToDevice, h->stream) !=
+        cudaSuccess) {
+        cleanup();
+        return mlp_err(h, KWG_ERR_CUDA, "kwg_mlp_train: parameter snapshot failed");
+    }
     for (int ep = 0; ep < epochs; ++ep) {
         std::shuffle(order.begin(), order.end(), rng);
         if (cudaMemcpyAsync(idx, order.data(), (size_t)n * 4, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
@@ -552,7 +558,7 @@ int kwg_mlp_train(kwg_mlp* h, const kwg_option* d_opts, const double* d_prices, 
             best = mean;
             h->best_epoch = ep;
             e = cudaMemcpyAsync(pbest, h->p, sizeof(float) * kMlpParams, cudaMemcpyDeviceToDevice, h->stream);
-        } else if (h->best_epoch >= 0 && !(mean <= kSpike * best)) {
+        } else if (!std::isfinite(mean) || !(mean <= kSpike * best)) {
             ++h->restarts;
             lr_scale *= 0.5f;
             h->adam_t = 0;
@@ -566,8 +572,9 @@ int kwg_mlp_train(kwg_mlp* h, const kwg_option* d_opts, const double* d_prices, 
             return mlp_err(h, KWG_ERR_CUDA, std::string("kwg_mlp_train: parameter snapshot: ") + cudaGetErrorString(e));
         }
     }
-    if (h->best_epoch >= 0 && h->best_epoch != epochs - 1) {
+    if (h->best_epoch != epochs - 1) {
         // the last epoch was not the best: its parameters give way to the best epoch's
+        // (or to the initial ones when no epoch had a finite loss)
         if (cudaMemcpyAsync(h->p, pbest, sizeof(float) * kMlpParams, cudaMemcpyDeviceToDevice, h->stream) !=
             cudaSuccess) {
             cleanup();

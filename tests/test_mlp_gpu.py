@@ -187,6 +187,44 @@ def test_training_reduces_loss(trained):
     assert after < 5e-3  # targets are scaled to unit standard deviation
 
 
+def test_training_recovers_from_loss_spikes(ctx):
+    """A learning rate far too large for Adam makes the loss blow up; the training
+    returns to its best epoch's parameters with fresh moments and half the rate each
+    time, and ends with finite parameters whose loss is the kept epoch's."""
+    import torch
+
+    import kwg
+    import portfolio
+
+    opts = portfolio.american_portfolio(4096, seed=202)
+    prices = _fd_prices(ctx, opts, t_dim=64, x_dim=128, scale=5.0, density=math.inf)
+    d_o = torch.from_numpy(opts.view(np.uint8).copy()).cuda()
+    d_p = torch.from_numpy(prices).cuda()
+    s = kwg.Surrogate(0, seed=4)
+    try:
+        # lr 1e4 overflows within the first epochs; halving 24 times brings it to ~6e-4
+        last = s.train(d_o.data_ptr(), d_p.data_ptr(), len(opts), epochs=24, batch=256, lr=1e4, seed=8)
+        h = s.train_history()
+        losses = h["losses"]
+        best, kept, restarts = math.inf, -1, 0  # the rule, replayed on the history
+        for i, v in enumerate(losses):
+            if np.isfinite(v) and v < best:
+                best, kept = v, i
+            elif not np.isfinite(v) or v > 3 * best:
+                restarts += 1
+        assert restarts >= 1
+        assert h["restarts"] == restarts and h["best_epoch"] == kept, (h, restarts, kept)
+        assert last == (losses[kept] if kept >= 0 else losses[-1])
+        p, _, _, _ = s.get_params()
+        assert np.isfinite(p).all()
+        d_out = torch.empty(len(opts), dtype=torch.float64, device="cuda")
+        s.price_device(d_o.data_ptr(), len(opts), d_out.data_ptr())
+        torch.cuda.synchronize()
+        assert torch.isfinite(d_out).all()
+    finally:
+        s.close()
+
+
 def test_training_keeps_the_best_epoch(trained):
     """The training history: one mean loss per epoch, the kept epoch is the one with
     the lowest loss, and the loss train() reports is that epoch's."""
