@@ -1,7 +1,7 @@
 // A minimal stand-in for the reference's pricer interface, written for the tests of
-// this repository so that the kw::Pricer subclasses given to a maintainer of the
-// reference can be compiled and run where the reference's sources
-// are absent.  It declares only what those subclasses use, with the signatures of
+// this repository so that the kw::Pricer subclasses of the integration guide (the
+// ones a maintainer of the reference would add) can be compiled and run where the
+// reference's sources are absent.  It declares only what those subclasses use, with the signatures of
 //   kw::Error                 src/Core/kwTypes.h:15     (std::string, empty = success)
 //   kw::Option                src/Core/kwAsset.h:12-22  (56-byte record)
 //   kw::Config::get / set     src/Core/kwConfig.h:21-73 (typed maps: real, integer, text)

@@ -1,6 +1,6 @@
-"""The kw::Pricer subclasses that INTEGRATION.md gives a maintainer of the reference
-(Fd1dGpu_Pricer, Fd1dBsGpu_Pricer), compiled verbatim from the document, linked
-against libkwg.so and run.
+"""The kw::Pricer subclasses the integration guide gives a maintainer of the reference
+(Fd1dGpu_Pricer, Fd1dBsGpu_Pricer), compiled verbatim from the guide, linked against
+libkwg.so and run.
 
 * Against the reference's own headers (src/Pricer/kwPricer.h, src/Core/kwConfig.h):
   init() succeeds on a GPU and reports the missing device without one.  Skipped
