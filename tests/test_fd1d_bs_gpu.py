@@ -152,3 +152,17 @@ def test_twin_tiles_qdfp_portfolio(ctx):
     rc, msg, want, _ = kwor.fd1d_price(g["opts"], bs=True, nthreads=16)
     assert rc == 0, msg
     assert (st == 0).all() and rel_err(p, want) <= REL_TOL
+
+
+def test_twin_tiles_repeat_bit_for_bit(ctx):
+    """Twin tiles under full load on the sinh grid (32768 options, 65536 PDEs, 1024
+    nodes, 48 levels): eight calls give the same bits."""
+    import portfolio
+
+    o = portfolio.american_portfolio(32768, seed=43)
+    kw = dict(t_dim=48, x_dim=1024, scale=5.0, density=0.25, solver=1)
+    first, st = bs_price(ctx, o, **kw)
+    assert (st == 0).all()
+    for _ in range(8):
+        again, st2 = bs_price(ctx, o, **kw)
+        assert (st2 == 0).all() and np.array_equal(again, first)

@@ -124,6 +124,24 @@ def test_uneven_graph_replay_and_duplicates(ctx):
     assert not np.array_equal(p3[:4], p3[4:])
 
 
+def test_uneven_replays_repeat_bit_for_bit(ctx):
+    """The streaming solver's big stages under load (one 4-warp block per SM, 16384
+    options of every node count, t_dim up to 128): eight graph replays give the same
+    bits.  Ring refills that overtook the lanes' reads of a slot showed as whole tiles
+    off on some runs."""
+    import kwg
+
+    o, xd, td = sample(16384, seed=21)
+    td = np.minimum(td, 128)
+    prm = kwg.params(scale=SCALE, density=math.inf, solver=1, block_warps=4, sm_blocks=1)
+    rc, first, st = ctx.fd1d_price_uneven(o, xd, td, prm)
+    assert rc == 0 and (st == 0).sum() > 0.8 * len(o)
+    for _ in range(8):
+        rc, again, st2 = ctx.fd1d_price_uneven(o, xd, td, prm)
+        assert rc == 0 and np.array_equal(st2, st)
+        assert np.array_equal(again[st == 0], first[st == 0])
+
+
 def test_uneven_rejects_bad_shapes(ctx):
     import kwg
 
