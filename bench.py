@@ -10,7 +10,7 @@ theta 0.5, scale 5, uniform x-grid, FP64 -- the reference's largest logged shape
 Reported on one JSON line (rank 0):
   value      options/s with inputs resident in HBM (kwg_fd1d_price_device), CUDA
              events on the launching stream, K steps after W warm-up steps; the
-             per-step working set (2.7 GB of coefficients and state) is far larger
+             per-step working set (2.4 GB of coefficients, payoff and state) is far larger
              than L2, so no flush is needed between steps.
   e2e        the same metric through the reference-facing call (kwg_fd1d_price: host
              options in, host prices out; dedup, H2D and D2H inside the timing).
