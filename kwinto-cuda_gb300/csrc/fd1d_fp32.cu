@@ -259,18 +259,16 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
             c2b = (float)(dt * a.ax / (x1 - x0));
             c3b = (float)(dt * a.ax / (g.x(N - 1) - g.x(N - 2)));
         }
-        // uniform grids: operator rows from the exact spacing, as the FP64 solvers build
-        // them; the interior row is the same at every interior node, so it is built once
-        // (three divisions per node fewer in this FP64 prologue)
-        const bool uni = kUni || sh.uniform;  // kUni: a uniform grid of full lanes
+        // uniform grids of full lanes (kUni): operator rows from the exact spacing, as the
+        // FP64 solvers build them; the interior row is the same at every interior node,
+        // so it is built once (three divisions per node fewer in this FP64 prologue).
+        // Compile-time only: the other instantiations keep their register budget.
+        constexpr bool uni = kUni;
         const double hxu = uni ? dvd(sub(g.xMax, g.xMin), (double)(N - 1)) : 0.;
         Row row_int{};
         bool have_int = false;
-        // other grids: rows from the reciprocal spacings the loops below carry from node
-        // to node (two divisions per node instead of three for the row and three for
-        // the residual coefficients)
-        auto row_at = [&](int j, double iu, double im, double id) -> Row {
-            if (!uni) return implicit_row_r(j, N, iu, im, id, sh.theta, dt, a.a0, a.ax, a.axx);
+        auto row_at = [&](int j, double xm, double x0, double xp) -> Row {
+            if (!uni) return implicit_row(j, N, xm, x0, xp, sh.theta, dt, a.a0, a.ax, a.axx);
             if (j == 0 || j == N - 1) return implicit_row(j, N, -hxu, 0., hxu, sh.theta, dt, a.a0, a.ax, a.axx);
             if (!have_int) row_int = implicit_row(j, N, -hxu, 0., hxu, sh.theta, dt, a.a0, a.ax, a.axx);
             have_int = true;
@@ -293,8 +291,6 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
             }
             double d_prev = 1., id_prev = 1., bu_prev = 0.;
             double pu = 1., pl = 1., sum = 0., fL = 0., bl_first = 0., pr = 1.;
-            // 1 / (x_j - x_{j-1}) of the current node (the previous node's upward reciprocal)
-            double r_d = (!kUni && j0 > 0 && j0 < N) ? 1. / (x0 - xm) : 0.;
 #pragma unroll 1
             for (int i = 0; i < M; ++i) {
                 const int j = j0 + i;
@@ -302,14 +298,8 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
                 double bl = 0., bb = 1., bu = 0.;
                 float c1 = 0.f, c2 = 0.f, c3 = 0.f, c4 = 0.f;
                 FF p = {0.f, 0.f};
-                double r_u = 0.;
                 if (j < N) {
-                    double r_m = 0.;
-                    if (!kUni) {
-                        if (j + 1 < N) r_u = 1. / (xp - x0);
-                        if (j > 0 && j + 1 < N) r_m = 1. / (xp - xm);
-                    }
-                    const Row rw = row_at(j, r_u, r_m, r_d);
+                    const Row rw = row_at(j, xm, x0, xp);
                     bl = rw.bl;
                     bb = rw.b;
                     bu = rw.bu;
@@ -319,7 +309,7 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
                     } else if (j == N - 1) {
                         c3 = (float)(dt * a.ax / (x0 - xm));
                     } else {
-                        const double iu = r_u, im = r_m, id = r_d;
+                        const double iu = 1. / (xp - x0), im = 1. / (xp - xm), id = 1. / (x0 - xm);
                         const double u2 = 2. * iu * im, l2 = 2. * id * im;
                         c1 = (float)(dt * a.axx * l2);
                         c2 = (float)(dt * (a.axx * (u2 - l2) + a.ax * im));
@@ -383,7 +373,6 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
                 bu_prev = bu;
                 xm = x0;
                 x0 = xp;
-                r_d = r_u;
             }
             (void)d_prev;
             L1 = bl_first * sum;
@@ -398,21 +387,13 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
             double e_next = 1., bl_next = 0.;
             const int jt = j0 + M - 1;
             double xp = (jt + 1 < N) ? g.x(jt + 1) : 0., x0 = (jt < N) ? g.x(jt) : 0.;
-            // 1 / (x_{j+1} - x_j) of the current node (the node above's downward reciprocal)
-            double r_u = (!uni && jt + 1 < N) ? 1. / (xp - x0) : 0.;
 #pragma unroll 1
             for (int i = M - 1; i > P; --i) {
                 const int j = j0 + i;
                 const double xm = (j - 1 < N) ? g.x(j - 1) : 0.;
                 double bl = 0., bb = 1., bu = 0.;
-                double r_d = 0.;
                 if (j < N) {
-                    double r_m = 0.;
-                    if (!uni && j > 0) {
-                        r_d = 1. / (x0 - xm);
-                        if (j + 1 < N) r_m = 1. / (xp - xm);
-                    }
-                    const Row rw = row_at(j, r_u, r_m, r_d);
+                    const Row rw = row_at(j, xm, x0, xp);
                     bl = rw.bl;
                     bb = rw.b;
                     bu = rw.bu;
@@ -428,7 +409,6 @@ __global__ void __launch_bounds__(32 * W) fd1d_solve_fp32(const PdeBatch b, Fd1d
                 bl_next = bl;
                 xp = x0;
                 x0 = xm;
-                r_u = r_d;
             }
             const double m_piv = (P == M - 1) ? 0. : bu_piv / e_next;
             const double gam = b_piv - l_piv * bu_above - m_piv * bl_next;
