@@ -65,6 +65,9 @@ def _cases():
         (_mixed(97, seed=12), kwg.params(t_dim=129, x_dim=257, scale=5.0, density=np.inf, solver=kwg.SOLVER_THOMAS)),
         (_mixed(301, seed=13), kwg.params(t_dim=200, x_dim=512, scale=5.0, density=0.25, solver=kwg.SOLVER_THOMAS,
                                           block_warps=2)),
+        # one 4-warp block per SM: the streaming solver's big stages
+        (_mixed(250, seed=14), kwg.params(t_dim=150, x_dim=640, scale=5.0, density=np.inf, solver=kwg.SOLVER_THOMAS,
+                                          block_warps=4, sm_blocks=1)),
     ]
 
 
