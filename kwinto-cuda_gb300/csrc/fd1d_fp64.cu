@@ -41,9 +41,9 @@
 //     S  [node][32][2]  state (V, h|f), one 16-byte load/store per lane
 // A sweep streams them in stages of consecutive nodes (one mbarrier, one to three
 // bulk copies per stage): 2 G nodes in the middle region, where the coefficients are
-// not read, G nodes elsewhere (G = 8, or 16 for launches with few warps per SM).  Where the payoff of every lane of the tile
-// is exactly +0 (the out-of-the-money
-// side of a tile of puts only or calls only; all nodes of European PDEs, which never
+// not read, G nodes elsewhere (G = 8, or 16 for launches with few warps per SM).
+// Where the payoff of every lane of the tile is exactly +0 (the out-of-the-money side
+// of a tile of puts only or calls only; all nodes of European PDEs, which never
 // project) the payoff is not read either: the projection there is max(V, +0).
 #include <atomic>
 #include <cstdint>
